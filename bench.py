@@ -1,0 +1,366 @@
+"""Benchmark: Gcell-updates/s of the GB300 FDTD solver on the 256x256x128 crystal.
+
+One bench step = one complete simulation of the seeded 256 x 256 x 128-cell
+crystal (257*257*129 = 8,520,321 mesh nodes, 2000 time steps, lattice a=16,
+radii U[0.2a, 0.4a], 25% tungsten, 42 MHz line source, uz surface recorded
+every 10 steps) starting from the zero state, on the FP32 Kahan path (the
+headline) with the plain FP64 path measured beside it on the same crystal.
+Gcell-updates/s = mesh nodes x time steps / s (nodes = (cells+1)^3, the
+reference's "points", tests/test_speed.py:52).
+
+value: device time (CUDA events on the solver's stream) with all state
+resident in HBM; the state (612 MB) is larger than L2.  e2e: wall time
+through the public API with pinned host buffers: per step the material ids
+and source go host->device and the surface records and final uz come back.
+
+--impl reference times the reference algorithm on the host cores: the C
+restatement of phonomena's NumPy solver (oracle/cpu_ref.c, FP64, bit-identical
+to the reference), all host threads, a bounded number of time steps per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+GRAPH_CHUNK = 12
+BYTES_PER_NODE = 73  # algorithmic: 3 components x (u, v, c) read + write x 4 B, + 1 B material id (FP64: u, u_old read, u_new write x 8 B + 1)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--fdtd-steps", type=int, default=2000)
+    p.add_argument("--cells", default="256,256,128")
+    p.add_argument("--tile-j", type=int, default=0)
+    p.add_argument("--x-segment", type=int, default=0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("pci.bus_id,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id):
+        self.bus = (bus_id or "").lower()[-12:]
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or (self.bus and not parts[0].lower().endswith(self.bus)):
+                continue
+            rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def graph_launches(nsteps):
+    full, rem = divmod(nsteps, GRAPH_CHUNK)
+    return full * (GRAPH_CHUNK + 1) + rem + (1 if rem else 0)
+
+
+def workload(cells, seed, fdtd_steps):
+    from phonomena_gb300 import crystal
+
+    spec = crystal.CrystalSpec(cells=cells, lattice=16, radius=(0.2, 0.4), depth=10, tungsten_frac=0.25,
+                               seed=seed, steps=fdtd_steps)
+    g, m = crystal.build(spec)
+    src = crystal.sin_source(spec.freq, m.dt, fdtd_steps)
+    return spec, g, m, src
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_node(kernel):
+    """DRAM bytes per node-update of a kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.load(open(p))
+    return d.get(kernel, {}).get("dram_bytes_per_node")
+
+
+def cpu_oracle_rate(cells, seconds, seed=0):
+    """FP64 reference restatement on all host threads: (Gcell-updates/s, threads, steps)."""
+    from oracle import cpu_oracle
+
+    spec, g, m, src = workload(cells, seed, 4096)
+    prob = cpu_oracle.OracleProblem(g.spacing(), m.ids, m.table, m.dt, src, surface_mode=1)
+    st = cpu_oracle.F64State(prob)
+    threads = cpu_oracle.max_threads()
+    cpu_oracle.run_f64(prob, st, t0=0, nsteps=1)  # warm caches / page in
+    done, t = 1, 0.0
+    while t < seconds and done < 4000:
+        t0 = time.perf_counter()
+        cpu_oracle.run_f64(prob, st, t0=done, nsteps=2)
+        t += time.perf_counter() - t0
+        done += 2
+    return spec.n_nodes * (done - 1) / t / 1e9, threads, done - 1, t
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    cells = tuple(int(c) for c in args.cells.split(","))
+    from oracle import cpu_oracle
+
+    spec, g, m, src = workload(cells, 0, 4096)
+    prob = cpu_oracle.OracleProblem(g.spacing(), m.ids, m.table, m.dt, src, surface_mode=1)
+    st = cpu_oracle.F64State(prob)
+    threads = cpu_oracle.max_threads()
+    per_step = 4  # time steps of the 256^2 x 128 crystal per bench step (bounded sample)
+    t_done = 0
+    for _ in range(args.warmup):
+        cpu_oracle.run_f64(prob, st, t0=t_done, nsteps=per_step)
+        t_done += per_step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_oracle.run_f64(prob, st, t0=t_done, nsteps=per_step)
+        t_done += per_step
+    el = time.perf_counter() - t0
+    val = spec.n_nodes * per_step * args.steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": round(val, 6), "unit": "Gcell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({spec.n_nodes} nodes), "
+                               f"{per_step} time steps per bench step (bounded sample of the 2000-step run)",
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(val, 6), "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step * args.steps} time steps of the {cells} crystal, FP64 reference "
+                                   "arithmetic (oracle/cpu_ref.c, OpenMP)"},
+        "e2e": {"value": round(val, 6), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from phonomena_gb300.device import DeviceSimulation
+
+    cells = tuple(int(c) for c in args.cells.split(","))
+    S = args.fdtd_steps
+    spec, g, m, src = workload(cells, rank, S)
+    nodes = spec.n_nodes
+    sp = g.spacing()
+    kw = dict(surface_mode="corrected", max_steps=S, record_every=10, tile_j=args.tile_j, x_segment=args.x_segment)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- FP32 Kahan: device-resident throughput ----
+    sim = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f32k", **kw)
+    sim.set_source(src)
+    stream = torch.cuda.ExternalStream(sim.stream_ptr)
+    for _ in range(args.warmup):
+        sim.reset()
+        sim.step(S)
+    sim.sync()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    bus = torch.cuda.get_device_properties(local).pci_bus_id if hasattr(torch.cuda.get_device_properties(local),
+                                                                         "pci_bus_id") else ""
+    with ClockSampler(bus) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            sim.reset()
+            sim.step(S)
+        e1.record(stream)
+        e1.synchronize()
+    sim.sync()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    barrier()
+    clocks = clk.summary()
+    value = world * nodes * S * args.steps / (ms / 1e3) / 1e9
+    surf32 = sim.read_surface().astype(np.float64)
+    u32 = [sim.download(k).astype(np.float64) for k in ("ux", "uy", "uz")]
+    e32 = sim.energy()
+    launch_ms = ms / (args.steps * S)
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_NODE * nodes / (launch_ms / 1e3) / 1e9
+    tpn = traffic_per_node("fdtd_step_kernel_f32k")
+
+    # ---- plain FP64 on the same crystal (one full run) ----
+    sim64 = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f64", **kw)
+    sim64.set_source(src)
+    s64 = torch.cuda.ExternalStream(sim64.stream_ptr)
+    sim64.step(GRAPH_CHUNK)
+    sim64.sync()
+    sim64.reset()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(s64)
+    sim64.step(S)
+    f1.record(s64)
+    f1.synchronize()
+    sim64.sync()
+    ms64 = max_over_ranks(f0.elapsed_time(f1))
+    value64 = world * nodes * S / (ms64 / 1e3) / 1e9
+    surf64 = sim64.read_surface()
+    u64 = [sim64.download(k) for k in ("ux", "uy", "uz")]
+    e64 = sim64.energy()
+    rel_surf = float(np.linalg.norm(surf32 - surf64) / np.linalg.norm(surf64))
+    rel_u = float(math.sqrt(sum(np.linalg.norm(a - b) ** 2 for a, b in zip(u32, u64)))
+                  / math.sqrt(sum(np.linalg.norm(b) ** 2 for b in u64)))
+    rel_e = float(abs(sum(e32) - sum(e64)) / abs(sum(e64)))
+    sim64.close()
+
+    # ---- e2e through the public API with pinned host buffers ----
+    def pinned(shape, dtype):
+        t = torch.empty(shape, dtype=dtype, pin_memory=True)
+        return t.numpy()
+
+    ids_h = pinned(m.ids.shape, torch.uint8)
+    ids_h[...] = m.ids
+    src_h = pinned(src.shape, torch.float64)
+    src_h[...] = src
+    nrec = S // 10
+    surf_h = pinned((nrec, g.x.size, g.y.size), torch.float32)
+    uz_h = pinned((g.x.size, g.y.size, g.z.size - 1), torch.float32)
+    h2d = ids_h.nbytes + m.table.nbytes + src_h.nbytes
+    d2h = surf_h.nbytes + uz_h.nbytes
+    for _ in range(max(1, min(args.warmup, 2))):
+        sim.set_materials(ids_h, m.table)
+        sim.set_source(src_h)
+        sim.reset()
+        sim.step(S)
+        sim.read_surface(0, nrec, out=surf_h)
+        sim.download("uz", out=uz_h)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.set_materials(ids_h, m.table)
+        sim.set_source(src_h)
+        sim.reset()
+        sim.step(S)
+        sim.read_surface(0, nrec, out=surf_h)
+        sim.download("uz", out=uz_h)
+    sim.sync()
+    wall = max_over_ranks(time.perf_counter() - t0)
+    e2e = world * nodes * S * args.steps / wall / 1e9
+    sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, threads, nst, secs = cpu_oracle_rate(cells, args.cpu_seconds)
+        cpu = {"value": round(rate, 6), "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{nst} time steps of the same crystal in {secs:.1f} s, FP64 reference arithmetic "
+                         "(oracle/cpu_ref.c, OpenMP, bit-identical to phonomena's solver_default)"}
+
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded crystal, one per rank)",
+            "config": {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({nodes} nodes), {S} time steps "
+                                   "per bench step from the zero state, FP32 velocity form with Kahan-compensated u, "
+                                   "corrected z=0 row, absorbing walls, uz surface every 10 steps",
+                       "nodes": nodes, "fdtd_steps": S, "l2": "inputs larger than L2 (state 612 MB)",
+                       "parallelism": f"replicas x{world}"},
+            "fp64": {"value": round(value64, 4), "unit": "Gcell-updates/s", "fdtd_steps": S,
+                     "ms": round(ms64, 3), "speedup_f32k_over_f64": round(value / value64, 3)},
+            "error_vs_fp64": {"rel_l2_surface_uz": rel_surf, "rel_l2_u": rel_u, "rel_energy": rel_e,
+                              "fdtd_steps": S},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+                         "traffic": (round(tpn * nodes) if tpn else None),
+                         "algorithmic_bytes_per_launch": BYTES_PER_NODE * nodes,
+                         "avg_launch_ms": round(launch_ms, 5)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": graph_launches(S) * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

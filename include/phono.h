@@ -1,0 +1,166 @@
+/*
+ * phono.h - C ABI of libphono_gpu.so, the GB300 (sm_103a) elastic FDTD
+ * solver that stands in for phonomena's time-stepping solver.
+ *
+ * The reference solver is the Python class BaseSolver
+ * (phonomena/simulation/base_solver.py:172-571) behind the plugin interface
+ * found by common.importSolver / findSolvers (phonomena/common.py:122-145).
+ * A plugin module (phonomena_gb300/solver_gb300.py) binds these entry points
+ * with ctypes; each declaration names the reference code it replaces.
+ *
+ * Conventions
+ *  - Plain C types only; host pointers unless a name says "dev".
+ *  - Every call returns PHONO_OK (0) or a negative PHONO_ERR_* code and
+ *    never aborts; phono_last_error() gives a message for the calling thread.
+ *  - A handle owns its device memory and one CUDA stream; calls on a handle
+ *    are ordered on that stream.  Use one handle per host thread.
+ *  - Arrays are C order with x slowest, in the reference shapes
+ *    (phonomena/simulation/grid.py:88-110): ux (nx-1, ny, nz),
+ *    uy (nx, ny-1, nz), uz (nx, ny, nz-1); nx, ny, nz are mesh NODE counts
+ *    (Grid.x.size, ...), each >= 3.
+ */
+#ifndef PHONO_H
+#define PHONO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHONO_ABI_VERSION 1
+
+#define PHONO_OK 0
+#define PHONO_ERR_ARG (-1)      /* invalid argument */
+#define PHONO_ERR_CUDA (-2)     /* CUDA runtime error */
+#define PHONO_ERR_NOMEM (-3)    /* device or host allocation failed / over budget */
+#define PHONO_ERR_STATE (-4)    /* call not valid in the current state */
+#define PHONO_ERR_NUMERIC (-5)  /* non-finite value seen in the recorded surface */
+
+/* arithmetic scheme */
+#define PHONO_F64 0  /* reference leapfrog, IEEE op order of the reference */
+#define PHONO_F32K 1 /* FP32 velocity form, Kahan-compensated displacement */
+
+/* z = 0 displacement row (base_solver.py:511-516) */
+#define PHONO_SURFACE_REFERENCE 0 /* precedence as written at :516 */
+#define PHONO_SURFACE_CORRECTED 1 /* (T3[...,1] - T3[...,0]) / fdz */
+
+/* the four walls x=N, y=0, y=N, z=N (base_solver.py:519-554) */
+#define PHONO_BC_ABSORBING 0 /* first-order absorbing faces, reference order */
+#define PHONO_BC_RIGID 1     /* u = 0 on those faces */
+
+/* source overwrite (base_solver.py:251) */
+#define PHONO_SOURCE_LINE 0 /* uz[0, :, 0] = s(tt) (reference) */
+#define PHONO_SOURCE_WALL 1 /* uz[0, :, :] = s(tt) */
+
+/* fields for phono_download / phono_upload */
+#define PHONO_FIELD_UX 0
+#define PHONO_FIELD_UY 1
+#define PHONO_FIELD_UZ 2
+#define PHONO_FIELD_UX_OLD 3 /* F64: u at the previous step */
+#define PHONO_FIELD_UY_OLD 4
+#define PHONO_FIELD_UZ_OLD 5
+#define PHONO_FIELD_VX 6 /* F32K: velocity at the last half step */
+#define PHONO_FIELD_VY 7
+#define PHONO_FIELD_VZ 8
+#define PHONO_FIELD_CX 9 /* F32K: Kahan compensation */
+#define PHONO_FIELD_CY 10
+#define PHONO_FIELD_CZ 11
+
+/* Material table row: C00 C01 C02 C10 C11 C12 C20 C21 C22 C33 C44 C55 rho.
+ * Replaces the per-node Material.C (nx,ny,nz,6,6) and Material.P arrays
+ * (phonomena/simulation/material.py:48-63) by one row per material id. */
+#define PHONO_TABLE_COLS 13
+
+typedef struct phono_desc {
+  int nx, ny, nz;                /* mesh nodes per axis, each >= 3 */
+  const double *fdx, *fdy, *fdz; /* full spacings, n-1 values (SI)  grid.py:117-120 */
+  const double *sdx, *sdy, *sdz; /* staggered spacings, n-2 values  grid.py:122-127 */
+  const uint8_t *mat;            /* nx*ny*nz node material ids */
+  const double *table;           /* nmat rows of PHONO_TABLE_COLS */
+  int nmat;                      /* 1..256 */
+  double dt;                     /* time step (Material.dt, material.py:80-93) */
+  int precision;                 /* PHONO_F64 | PHONO_F32K */
+  int surface_mode;              /* PHONO_SURFACE_* */
+  int bc;                        /* PHONO_BC_* */
+  int source_mode;               /* PHONO_SOURCE_* */
+  int max_steps;                 /* capacity: source samples and surface records */
+  int record_every;              /* record uz[:, :, 0] after every k-th step; 0 = off */
+  int tile_j;                    /* tile height along y: 4, 8 or 16; 0 = default */
+  int x_segment;                 /* planes per tile column segment; 0 = default */
+} phono_desc;
+
+typedef struct phono_handle phono_handle;
+
+/* Allocate the device state (zero fields) for one simulation.
+ * Replaces BaseSolver.init (base_solver.py:194-222). */
+int phono_create(const phono_desc *desc, phono_handle **out);
+
+/* Source sample s(tt) of every global step tt < n (n <= max_steps): the value
+ * the reference writes into uz[0,:,0] before step tt (base_solver.py:251),
+ * from update_sin / update_ricker (base_solver.py:294-312). */
+int phono_set_source(phono_handle *h, const double *samples, int n);
+
+/* Advance nsteps time steps; one fused kernel launch per step, replayed from
+ * a captured CUDA graph.  Replaces the loop body of BaseSolver.run
+ * (base_solver.py:245-266): source, update_T, update_T_BC, update_u,
+ * update_u_BC, time_step.  Asynchronous on the handle's stream. */
+int phono_step(phono_handle *h, int nsteps);
+
+/* Global steps completed so far (host-side count of enqueued steps). */
+int phono_steps_done(const phono_handle *h);
+
+/* Zero the state, the surface records and the step counter: the handle is
+ * as after phono_create (material, spacing and source kept).  Stands in for
+ * the field allocation of Grid.update (grid.py:87-110) on a re-run. */
+int phono_reset(phono_handle *h);
+
+/* Replace the material ids and table of a handle (same mesh shape): a new
+ * crystal in an existing slot.  Replaces Material.setConstants
+ * (material.py:55-63) on the device. */
+int phono_set_materials(phono_handle *h, const uint8_t *mat, const double *table, int nmat);
+
+/* The handle's cudaStream_t (as void*), for callers that record their own
+ * CUDA events around phono_step. */
+void *phono_stream(phono_handle *h);
+
+/* Wait for the handle's stream; returns PHONO_ERR_NUMERIC if a recorded
+ * surface value was not finite. */
+int phono_sync(phono_handle *h);
+
+/* Copy surface records [first, first+count) to host: count * nx * ny values
+ * (double for PHONO_F64, float for PHONO_F32K), record r = uz[:, :, 0]
+ * after global step (r+1)*record_every - 1.  Stands in for the per-step
+ * uz dataset of the reference writer (base_solver.py:114-116,153-155). */
+int phono_read_surface(phono_handle *h, int first, int count, void *host_out);
+
+/* Copy a field of the current state to / from host (reference shape, element
+ * size 8 for PHONO_F64 and 4 for PHONO_F32K).  Download of UX..UZ is what
+ * the reference leaves in g.ux, g.uy, g.uz after run. */
+int phono_download(phono_handle *h, int field, void *host, size_t bytes);
+int phono_upload(phono_handle *h, int field, const void *host, size_t bytes);
+
+/* Element size in bytes of the handle's fields (8 or 4). */
+int phono_elem_size(const phono_handle *h);
+
+/* Kinetic and strain energy of the current state, FP64 accumulation:
+ * out[0] = sum rho v^2 / 2 * dV, out[1] = sum T:e / 2 * dV.  No reference
+ * counterpart (error metric). */
+int phono_energy(phono_handle *h, double out[2]);
+
+/* Device time of the last phono_step call in milliseconds (CUDA events). */
+int phono_last_step_ms(phono_handle *h, float *ms);
+
+void phono_destroy(phono_handle *h);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *phono_last_error(void);
+
+int phono_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHONO_H */

@@ -1,0 +1,94 @@
+"""ctypes binding of libphono_gpu.so (include/phono.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libphono_gpu.so"
+
+PHONO_OK = 0
+ERRORS = {-1: "PHONO_ERR_ARG", -2: "PHONO_ERR_CUDA", -3: "PHONO_ERR_NOMEM", -4: "PHONO_ERR_STATE",
+          -5: "PHONO_ERR_NUMERIC"}
+
+PRECISIONS = {"f64": 0, "f32k": 1}
+SURFACE_MODES = {"reference": 0, "corrected": 1}
+BCS = {"absorbing": 0, "reference": 0, "rigid": 1}
+SOURCE_MODES = {"line": 0, "wall": 1}
+FIELDS = {"ux": 0, "uy": 1, "uz": 2, "ux_old": 3, "uy_old": 4, "uz_old": 5,
+          "vx": 6, "vy": 7, "vz": 8, "cx": 9, "cy": 10, "cz": 11}
+
+# exported symbols of include/phono.h (checked by the CPU test suite)
+EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done", "phono_reset",
+           "phono_set_materials", "phono_stream", "phono_sync",
+           "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
+           "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
+
+
+class PhonoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PhonoDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("fdx", ctypes.c_void_p), ("fdy", ctypes.c_void_p), ("fdz", ctypes.c_void_p),
+        ("sdx", ctypes.c_void_p), ("sdy", ctypes.c_void_p), ("sdz", ctypes.c_void_p),
+        ("mat", ctypes.c_void_p), ("table", ctypes.c_void_p), ("nmat", ctypes.c_int),
+        ("dt", ctypes.c_double),
+        ("precision", ctypes.c_int), ("surface_mode", ctypes.c_int), ("bc", ctypes.c_int),
+        ("source_mode", ctypes.c_int), ("max_steps", ctypes.c_int), ("record_every", ctypes.c_int),
+        ("tile_j", ctypes.c_int), ("x_segment", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load the library (once); raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with phonomena_gb300.build.build() (nvcc, sm_103a)")
+    L = ctypes.CDLL(str(p))
+    vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    sig = {
+        "phono_create": (ci, [ctypes.POINTER(PhonoDesc), ctypes.POINTER(vp)]),
+        "phono_set_source": (ci, [vp, vp, ci]),
+        "phono_step": (ci, [vp, ci]),
+        "phono_steps_done": (ci, [vp]),
+        "phono_reset": (ci, [vp]),
+        "phono_set_materials": (ci, [vp, vp, vp, ci]),
+        "phono_stream": (vp, [vp]),
+        "phono_sync": (ci, [vp]),
+        "phono_read_surface": (ci, [vp, ci, ci, vp]),
+        "phono_download": (ci, [vp, ci, vp, ctypes.c_size_t]),
+        "phono_upload": (ci, [vp, ci, vp, ctypes.c_size_t]),
+        "phono_elem_size": (ci, [vp]),
+        "phono_energy": (ci, [vp, vp]),
+        "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
+        "phono_destroy": (None, [vp]),
+        "phono_last_error": (ctypes.c_char_p, []),
+        "phono_abi_version": (ci, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != PHONO_OK:
+        msg = _lib.phono_last_error().decode(errors="replace") if _lib is not None else ""
+        raise PhonoError(rc, msg)
+    return rc

@@ -1,0 +1,614 @@
+// C ABI of libphono_gpu.so (declared in include/phono.h).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/phono.h"
+#include "fdtd_common.cuh"
+
+namespace phono {
+cudaError_t configure_step_f64(int tj);
+cudaError_t configure_step_f32k(int tj);
+cudaError_t launch_step_f64(const StepArgs<double>& a, int tj, int n_face_blocks, cudaStream_t st);
+cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int n_face_blocks, cudaStream_t st);
+cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st);
+
+__global__ void advance_step_kernel(int* p, int n) { *p += n; }
+}  // namespace phono
+
+using namespace phono;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static const int kGraphSteps = 12;  // multiple of 2 and 3: buffer rotations line up
+static const int kEnergyBlocks = 1024;
+
+struct phono_handle {
+  phono_desc d;  // scalar copy; pointers not kept
+  int es = 8;
+  Geo g{};
+  size_t field_elems = 0;  // per array
+  size_t mat_bytes = 0;
+  std::vector<void*> allocs;
+  void* u[3][3] = {};
+  void* v[2][3] = {};
+  void* c[2][3] = {};
+  void* sp[6] = {};       // R spacings (F64 raw, F32K reciprocals)
+  double* sp64[6] = {};   // raw double spacings (energy)
+  double h_sp0[6] = {};   // first elements (raw)
+  std::vector<double> sp_host[6];  // raw spacings (ABC coefficients)
+  uint8_t* mat = nullptr;
+  void* tab = nullptr;       // 16 R per material
+  double* tab13 = nullptr;   // raw table (energy)
+  double* src = nullptr;
+  int nsrc = 0;
+  void* surf = nullptr;
+  int nrec_cap = 0;
+  int* step_base = nullptr;
+  int* err = nullptr;
+  double2* partial = nullptr;
+  double* energy_out = nullptr;
+  double abc[8] = {};
+  int tj = 8, xseg = 64, ntj = 0, ntk = 0, nseg = 0, n_tile = 0, n_face = 0;
+  FaceTable faces{};
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int steps_done = 0;
+  int nmat = 0;
+  bool timed = false;
+};
+
+static long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
+
+static int dalloc(phono_handle* h, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(PHONO_ERR_NOMEM, std::string("cudaMalloc ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+  }
+  h->allocs.push_back(*p);
+  return PHONO_OK;
+}
+
+static void release(phono_handle* h) {
+  if (!h) return;
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+// ABC coefficients in the reference order from the material at node (0,0,0)
+// (base_solver.py:525-537): clx[-1] ctx[-1] cty[0] cly[0] cty[-1] cly[-1] ctz[-1] clz[-1]
+static void abc_coeffs(const phono_handle* h, const double* row0, double out[8]) {
+  double vl = std::sqrt(row0[0] / row0[12]);
+  double vt = std::sqrt(row0[9] / row0[12]);
+  double vld = vl * h->d.dt, vtd = vt * h->d.dt;
+  const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
+  const std::vector<double>&fdx = h->sp_host[0], &fdy = h->sp_host[1], &fdz = h->sp_host[2];
+  const std::vector<double>&sdx = h->sp_host[3], &sdy = h->sp_host[4], &sdz = h->sp_host[5];
+  out[0] = (vld - sdx[nx - 3]) / (vld + sdx[nx - 3]);
+  out[1] = (vtd - fdx[nx - 2]) / (vtd + fdx[nx - 2]);
+  out[2] = (vtd - fdy[0]) / (vtd + fdy[0]);
+  out[3] = (vld - sdy[0]) / (vld + sdy[0]);
+  out[4] = (vtd - fdy[ny - 2]) / (vtd + fdy[ny - 2]);
+  out[5] = (vld - sdy[ny - 3]) / (vld + sdy[ny - 3]);
+  out[6] = (vtd - fdz[nz - 2]) / (vtd + fdz[nz - 2]);
+  out[7] = (vld - sdz[nz - 3]) / (vld + sdz[nz - 3]);
+}
+
+static int check_materials(const phono_handle* h, const uint8_t* mat, const double* table, int nmat) {
+  if (!mat || !table) return fail(PHONO_ERR_ARG, "material ids or table is NULL");
+  if (nmat < 1 || nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
+  for (int q = 0; q < nmat * PHONO_TABLE_COLS; q++)
+    if (!std::isfinite(table[q])) return fail(PHONO_ERR_ARG, "material table holds a non-finite value");
+  for (int q = 0; q < nmat; q++)
+    if (!(table[q * PHONO_TABLE_COLS + 12] > 0.0)) return fail(PHONO_ERR_ARG, "density must be > 0");
+  size_t n = (size_t)h->d.nx * h->d.ny * h->d.nz;
+  for (size_t q = 0; q < n; q++)
+    if (mat[q] >= nmat) return fail(PHONO_ERR_ARG, "material id out of range");
+  return PHONO_OK;
+}
+
+// ids into the padded layout, 16-entry device rows, raw rows, ABC coefficients
+static int upload_materials(phono_handle* h, const uint8_t* mat, const double* table, int nmat) {
+  const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr((void*)mat, nz, nz, ny);
+  p.dstPtr = make_cudaPitchedPtr(h->mat + h->g.mo0, h->g.msy, h->g.msy, ny + 2);
+  p.extent = make_cudaExtent(nz, ny, nx);
+  p.kind = cudaMemcpyHostToDevice;
+  CK(cudaMemcpy3DAsync(&p, h->stream));
+  const double dt = h->d.dt;
+  const double dt2 = dt * dt;
+  if (h->es == 8) {
+    std::vector<double> t(16 * nmat, 0.0);
+    for (int m = 0; m < nmat; m++) {
+      const double* row = table + m * PHONO_TABLE_COLS;
+      for (int q = 0; q < 12; q++) t[m * 16 + q] = row[q];
+      t[m * 16 + 12] = dt2 / row[12];  // (dt**2 / P) of base_solver.py:443
+      t[m * 16 + 13] = row[12];
+      t[m * 16 + 14] = dt;
+    }
+    CK(cudaMemcpyAsync(h->tab, t.data(), t.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  } else {
+    std::vector<float> t(16 * nmat, 0.0f);
+    for (int m = 0; m < nmat; m++) {
+      const double* row = table + m * PHONO_TABLE_COLS;
+      for (int q = 0; q < 12; q++) t[m * 16 + q] = (float)row[q];
+      t[m * 16 + 12] = (float)(dt / row[12]);
+      t[m * 16 + 13] = (float)row[12];
+      t[m * 16 + 14] = (float)dt;
+    }
+    CK(cudaMemcpyAsync(h->tab, t.data(), t.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  CK(cudaMemcpyAsync(h->tab13, table, (size_t)nmat * PHONO_TABLE_COLS * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->nmat = nmat;
+  abc_coeffs(h, table + (size_t)mat[0] * PHONO_TABLE_COLS, h->abc);
+  return PHONO_OK;
+}
+
+template <class R>
+static StepArgs<R> make_args(const phono_handle* h, int step_off) {
+  StepArgs<R> a{};
+  a.g = h->g;
+  a.sp.fdx = (const R*)h->sp[0];
+  a.sp.fdy = (const R*)h->sp[1];
+  a.sp.fdz = (const R*)h->sp[2];
+  a.sp.sdx = (const R*)h->sp[3];
+  a.sp.sdy = (const R*)h->sp[4];
+  a.sp.sdz = (const R*)h->sp[5];
+  R s0[6];
+  for (int q = 0; q < 6; q++) s0[q] = sizeof(R) == 8 ? (R)h->h_sp0[q] : (R)(1.0 / h->h_sp0[q]);
+  a.sp.fdx0 = s0[0];
+  a.sp.fdy0 = s0[1];
+  a.sp.fdz0 = s0[2];
+  a.sp.sdx0 = s0[3];
+  a.sp.sdy0 = s0[4];
+  a.sp.sdz0 = s0[5];
+  a.mat = h->mat;
+  a.tab = (const R*)h->tab;
+  a.src = h->src;
+  a.nsrc = h->nsrc;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) a.u[r][c] = (R*)h->u[r][c];
+  for (int r = 0; r < 2; r++)
+    for (int c = 0; c < 3; c++) {
+      a.v[r][c] = (R*)h->v[r][c];
+      a.c[r][c] = (R*)h->c[r][c];
+    }
+  for (int q = 0; q < 8; q++) a.abc[q] = (R)h->abc[q];
+  a.surf = (R*)h->surf;
+  a.record_every = h->d.record_every;
+  a.rec_base = 0;
+  a.nrec_cap = h->nrec_cap;
+  a.step_base = h->step_base;
+  a.step_off = step_off;
+  a.surface_mode = h->d.surface_mode;
+  a.bc = h->d.bc;
+  a.source_mode = h->d.source_mode;
+  a.ntj = h->ntj;
+  a.ntk = h->ntk;
+  a.nseg = h->nseg;
+  a.xseg = h->xseg;
+  a.n_tile_blocks = h->n_tile;
+  a.faces = h->faces;
+  a.err = h->err;
+  return a;
+}
+
+static cudaError_t launch_one(phono_handle* h, int step_off) {
+  if (h->d.precision == PHONO_F64) return launch_step_f64(make_args<double>(h, step_off), h->tj, h->n_face, h->stream);
+  return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->n_face, h->stream);
+}
+
+static int check_desc(const phono_desc* d) {
+  if (!d) return fail(PHONO_ERR_ARG, "desc is NULL");
+  if (d->nx < 3 || d->ny < 3 || d->nz < 3) return fail(PHONO_ERR_ARG, "nx, ny, nz must be >= 3 mesh nodes");
+  if ((long long)d->nx * d->ny * d->nz > (1LL << 34)) return fail(PHONO_ERR_ARG, "grid too large");
+  if (!d->fdx || !d->fdy || !d->fdz || !d->sdx || !d->sdy || !d->sdz) return fail(PHONO_ERR_ARG, "spacing array is NULL");
+  if (!d->mat || !d->table) return fail(PHONO_ERR_ARG, "material ids or table is NULL");
+  if (d->nmat < 1 || d->nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
+  if (d->precision != PHONO_F64 && d->precision != PHONO_F32K) return fail(PHONO_ERR_ARG, "unknown precision");
+  if (d->surface_mode < 0 || d->surface_mode > 1) return fail(PHONO_ERR_ARG, "unknown surface_mode");
+  if (d->bc < 0 || d->bc > 1) return fail(PHONO_ERR_ARG, "unknown bc");
+  if (d->source_mode < 0 || d->source_mode > 1) return fail(PHONO_ERR_ARG, "unknown source_mode");
+  if (d->max_steps < 0 || d->record_every < 0) return fail(PHONO_ERR_ARG, "max_steps and record_every must be >= 0");
+  if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return fail(PHONO_ERR_ARG, "dt must be finite and > 0");
+  if (d->tile_j != 0 && d->tile_j != 4 && d->tile_j != 8 && d->tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
+  if (d->x_segment < 0) return fail(PHONO_ERR_ARG, "x_segment must be >= 0");
+  for (int q = 0; q < d->nmat * PHONO_TABLE_COLS; q++)
+    if (!std::isfinite(d->table[q])) return fail(PHONO_ERR_ARG, "material table holds a non-finite value");
+  for (int q = 0; q < d->nmat; q++)
+    if (!(d->table[q * PHONO_TABLE_COLS + 12] > 0.0)) return fail(PHONO_ERR_ARG, "density must be > 0");
+  const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
+  int lens[6] = {d->nx - 1, d->ny - 1, d->nz - 1, d->nx - 2, d->ny - 2, d->nz - 2};
+  for (int a = 0; a < 6; a++)
+    for (int q = 0; q < lens[a]; q++)
+      if (!(arrs[a][q] > 0.0) || !std::isfinite(arrs[a][q])) return fail(PHONO_ERR_ARG, "spacings must be finite and > 0");
+  size_t n = (size_t)d->nx * d->ny * d->nz;
+  for (size_t q = 0; q < n; q++)
+    if (d->mat[q] >= d->nmat) return fail(PHONO_ERR_ARG, "material id out of range");
+  return PHONO_OK;
+}
+
+// 3-D copy between a dense host array (ex, ey, ez) and the padded device layout
+static cudaError_t copy3d(phono_handle* h, void* dev, void* host, int c, bool to_dev) {
+  int ex = h->d.nx - (c == 0), ey = h->d.ny - (c == 1), ez = h->d.nz - (c == 2);
+  cudaMemcpy3DParms p{};
+  cudaPitchedPtr hp = make_cudaPitchedPtr(host, (size_t)ez * h->es, (size_t)ez * h->es, ey);
+  cudaPitchedPtr dp = make_cudaPitchedPtr((char*)dev + h->g.o0 * h->es, (size_t)h->g.sy * h->es,
+                                          (size_t)h->g.sy * h->es, h->d.ny + 2);
+  p.extent = make_cudaExtent((size_t)ez * h->es, ey, ex);
+  if (to_dev) {
+    p.srcPtr = hp;
+    p.dstPtr = dp;
+    p.kind = cudaMemcpyHostToDevice;
+  } else {
+    p.srcPtr = dp;
+    p.dstPtr = hp;
+    p.kind = cudaMemcpyDeviceToHost;
+  }
+  cudaError_t e = cudaMemcpy3DAsync(&p, h->stream);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(h->stream);
+}
+
+// buffers holding the current state after steps_done steps
+static void* field_ptr(phono_handle* h, int field) {
+  int t = h->steps_done;
+  int comp = field % 3;
+  if (h->d.precision == PHONO_F64) {
+    if (field <= PHONO_FIELD_UZ) return h->u[(t + 1) % 3][comp];
+    if (field <= PHONO_FIELD_UZ_OLD) return h->u[t % 3][comp];
+    return nullptr;
+  }
+  int b = t & 1;
+  if (field <= PHONO_FIELD_UZ) return h->u[b][comp];
+  if (field <= PHONO_FIELD_UZ_OLD) return nullptr;
+  if (field <= PHONO_FIELD_VZ) return h->v[b][comp];
+  if (field <= PHONO_FIELD_CZ) return h->c[b][comp];
+  return nullptr;
+}
+
+extern "C" {
+
+int phono_abi_version(void) { return PHONO_ABI_VERSION; }
+
+const char* phono_last_error(void) { return g_err.c_str(); }
+
+int phono_create(const phono_desc* d, phono_handle** out) {
+  if (!out) return fail(PHONO_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int rc = check_desc(d);
+  if (rc) return rc;
+  phono_handle* h = new phono_handle();
+  h->d = *d;
+  h->d.fdx = h->d.fdy = h->d.fdz = h->d.sdx = h->d.sdy = h->d.sdz = nullptr;
+  h->d.mat = nullptr;
+  h->d.table = nullptr;
+  const bool f64 = d->precision == PHONO_F64;
+  h->es = f64 ? 8 : 4;
+  const int nx = d->nx, ny = d->ny, nz = d->nz;
+  // padded layout: planes -1..nx, rows -1..ny, 32-byte front pad in z
+  const long long koff = 32 / h->es;
+  const long long pz = round_up(koff + nz + 1, 128 / h->es);
+  h->g.nx = nx;
+  h->g.ny = ny;
+  h->g.nz = nz;
+  h->g.sy = pz;
+  h->g.sx = (long long)(ny + 2) * pz;
+  h->g.o0 = h->g.sx + h->g.sy + koff;
+  h->field_elems = (size_t)(nx + 2) * h->g.sx;
+  const long long mpz = round_up(nz + 2, 16);
+  h->g.msy = mpz;
+  h->g.msx = (long long)(ny + 2) * mpz;
+  h->g.mo0 = h->g.msx + h->g.msy + 1;
+  h->mat_bytes = (size_t)(nx + 2) * h->g.msx;
+
+  // tiles
+  h->tj = d->tile_j ? d->tile_j : 8;
+  h->xseg = d->x_segment ? d->x_segment : 64;
+  h->ntj = (ny - 1 + h->tj - 1) / h->tj;
+  h->ntk = (nz - 1 + TK - 1) / TK;
+  h->nseg = (nx - 1 + h->xseg - 1) / h->xseg;
+  long long ntile = (long long)h->ntj * h->ntk * h->nseg;
+  // faces: per component z=N (ex*ey), y=N and y=0 (ex*(ez-1)), x=N ((ey-2)*(ez-1))
+  long long acc = 0;
+  for (int c = 0; c < 3; c++) {
+    long long ex = nx - (c == 0), ey = ny - (c == 1), ez = nz - (c == 2);
+    long long cnt[4] = {ex * ey, ex * (ez - 1), ex * (ez - 1), (ey - 2) * (ez - 1)};
+    for (int p = 0; p < 4; p++) {
+      h->faces.off[c * 4 + p] = (int)acc;
+      acc += cnt[p];
+    }
+  }
+  h->faces.off[12] = (int)acc;
+  int nt = TK * h->tj;
+  long long nface = (acc + nt - 1) / nt;
+  if (ntile + nface > 0x7fffffffLL || acc > 0x7fffffffLL) {
+    delete h;
+    return fail(PHONO_ERR_ARG, "grid too large for one launch");
+  }
+  h->n_tile = (int)ntile;
+  h->n_face = (int)nface;
+
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return fail(PHONO_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+#define TRY(x)            \
+  do {                    \
+    int r_ = (x);         \
+    if (r_) {             \
+      std::string m_ = g_err; \
+      release(h);         \
+      g_err = m_;         \
+      return r_;          \
+    }                     \
+  } while (0)
+#define TRYC(x)                                                                         \
+  do {                                                                                  \
+    cudaError_t e_ = (x);                                                               \
+    if (e_ != cudaSuccess) {                                                            \
+      release(h);                                                                       \
+      return fail(PHONO_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
+    }                                                                                   \
+  } while (0)
+  TRYC(f64 ? configure_step_f64(h->tj) : configure_step_f32k(h->tj));
+  TRYC(cudaEventCreate(&h->ev0));
+  TRYC(cudaEventCreate(&h->ev1));
+  const size_t fb = h->field_elems * h->es;
+  if (f64) {
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) TRY(dalloc(h, &h->u[r][c], fb));
+  } else {
+    for (int r = 0; r < 2; r++)
+      for (int c = 0; c < 3; c++) {
+        TRY(dalloc(h, &h->u[r][c], fb));
+        TRY(dalloc(h, &h->v[r][c], fb));
+        TRY(dalloc(h, &h->c[r][c], fb));
+      }
+  }
+  for (void* p : h->allocs) TRYC(cudaMemsetAsync(p, 0, fb, h->stream));
+
+  // spacings
+  const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
+  int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
+  for (int a = 0; a < 6; a++) {
+    h->h_sp0[a] = arrs[a][0];
+    h->sp_host[a].assign(arrs[a], arrs[a] + lens[a]);
+    TRY(dalloc(h, &h->sp[a], (size_t)lens[a] * h->es));
+    TRY(dalloc(h, (void**)&h->sp64[a], (size_t)lens[a] * 8));
+    TRYC(cudaMemcpy(h->sp64[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    if (f64) {
+      TRYC(cudaMemcpy(h->sp[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    } else {
+      std::vector<float> r(lens[a]);
+      for (int q = 0; q < lens[a]; q++) r[q] = (float)(1.0 / arrs[a][q]);
+      TRYC(cudaMemcpy(h->sp[a], r.data(), (size_t)lens[a] * 4, cudaMemcpyHostToDevice));
+    }
+  }
+  // materials: padded id layout and the 16-entry device rows (capacity 256 ids)
+  TRY(dalloc(h, (void**)&h->mat, h->mat_bytes));
+  TRYC(cudaMemset(h->mat, 0, h->mat_bytes));
+  TRY(dalloc(h, &h->tab, (size_t)256 * 16 * h->es));
+  TRY(dalloc(h, (void**)&h->tab13, (size_t)256 * PHONO_TABLE_COLS * 8));
+  TRY(upload_materials(h, d->mat, d->table, d->nmat));
+  // source table, surface records, counters
+  int cap = d->max_steps > 0 ? d->max_steps : 1;
+  TRY(dalloc(h, (void**)&h->src, (size_t)cap * 8));
+  TRYC(cudaMemset(h->src, 0, (size_t)cap * 8));
+  h->nrec_cap = d->record_every > 0 ? d->max_steps / d->record_every : 0;
+  if (h->nrec_cap > 0) {
+    size_t sb = (size_t)h->nrec_cap * nx * ny * h->es;
+    TRY(dalloc(h, &h->surf, sb));
+    TRYC(cudaMemsetAsync(h->surf, 0, sb, h->stream));
+  }
+  TRY(dalloc(h, (void**)&h->step_base, sizeof(int) * 2));
+  h->err = h->step_base + 1;
+  TRYC(cudaMemsetAsync(h->step_base, 0, sizeof(int) * 2, h->stream));
+  TRY(dalloc(h, (void**)&h->partial, sizeof(double2) * kEnergyBlocks));
+  TRY(dalloc(h, (void**)&h->energy_out, sizeof(double) * 2));
+  TRYC(cudaStreamSynchronize(h->stream));
+#undef TRY
+#undef TRYC
+  *out = h;
+  return PHONO_OK;
+}
+
+int phono_set_source(phono_handle* h, const double* samples, int n) {
+  if (!h || (!samples && n > 0)) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (n < 0 || n > (h->d.max_steps > 0 ? h->d.max_steps : 1)) return fail(PHONO_ERR_ARG, "n exceeds max_steps");
+  for (int q = 0; q < n; q++)
+    if (!std::isfinite(samples[q])) return fail(PHONO_ERR_ARG, "source sample is not finite");
+  CK(cudaMemcpyAsync(h->src, samples, (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->nsrc = n;
+  return PHONO_OK;
+}
+
+static int build_graph(phono_handle* h) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < kGraphSteps && e == cudaSuccess; s++) e = launch_one(h, s);
+  if (e == cudaSuccess) {
+    advance_step_kernel<<<1, 1, 0, h->stream>>>(h->step_base, kGraphSteps);
+    e = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(PHONO_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  }
+  if (e2 != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e2));
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return PHONO_OK;
+}
+
+int phono_step(phono_handle* h, int nsteps) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (nsteps < 0) return fail(PHONO_ERR_ARG, "nsteps < 0");
+  if (h->steps_done + nsteps > h->nsrc)
+    return fail(PHONO_ERR_STATE, "not enough source samples: call phono_set_source with max_steps samples");
+  if (nsteps == 0) return PHONO_OK;
+  if (!h->graph && nsteps >= kGraphSteps) {
+    int rc = build_graph(h);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(h->ev0, h->stream));
+  int full = nsteps / kGraphSteps, rem = nsteps % kGraphSteps;
+  for (int q = 0; q < full; q++) CK(cudaGraphLaunch(h->graph, h->stream));
+  for (int s = 0; s < rem; s++) CK(launch_one(h, s));
+  if (rem) {
+    advance_step_kernel<<<1, 1, 0, h->stream>>>(h->step_base, rem);
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(h->ev1, h->stream));
+  h->timed = true;
+  h->steps_done += nsteps;
+  return PHONO_OK;
+}
+
+int phono_steps_done(const phono_handle* h) { return h ? h->steps_done : fail(PHONO_ERR_ARG, "handle is NULL"); }
+
+int phono_sync(phono_handle* h) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  CK(cudaStreamSynchronize(h->stream));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return fail(PHONO_ERR_NUMERIC, "non-finite value in the recorded surface");
+  return PHONO_OK;
+}
+
+int phono_last_step_ms(phono_handle* h, float* ms) {
+  if (!h || !ms) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (!h->timed) return fail(PHONO_ERR_STATE, "no step timed yet");
+  CK(cudaEventSynchronize(h->ev1));
+  CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
+  return PHONO_OK;
+}
+
+int phono_read_surface(phono_handle* h, int first, int count, void* host_out) {
+  if (!h || (!host_out && count > 0)) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (first < 0 || count < 0 || first + count > h->nrec_cap) return fail(PHONO_ERR_ARG, "record range out of bounds");
+  if (count == 0) return PHONO_OK;
+  size_t rec = (size_t)h->d.nx * h->d.ny * h->es;
+  CK(cudaMemcpyAsync(host_out, (char*)h->surf + (size_t)first * rec, (size_t)count * rec, cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return PHONO_OK;
+}
+
+static int field_check(phono_handle* h, int field, const void* host, size_t bytes, void** dev) {
+  if (!h || !host) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (field < 0 || field > PHONO_FIELD_CZ) return fail(PHONO_ERR_ARG, "unknown field");
+  *dev = field_ptr(h, field);
+  if (!*dev) return fail(PHONO_ERR_ARG, "field not held by this precision");
+  int c = field % 3;
+  size_t n = (size_t)(h->d.nx - (c == 0)) * (h->d.ny - (c == 1)) * (h->d.nz - (c == 2));
+  if (bytes != n * h->es) return fail(PHONO_ERR_ARG, "byte count does not match the field shape");
+  return PHONO_OK;
+}
+
+int phono_download(phono_handle* h, int field, void* host, size_t bytes) {
+  void* dev;
+  int rc = field_check(h, field, host, bytes, &dev);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(copy3d(h, dev, host, field % 3, false));
+  return PHONO_OK;
+}
+
+int phono_upload(phono_handle* h, int field, const void* host, size_t bytes) {
+  void* dev;
+  int rc = field_check(h, field, host, bytes, &dev);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(copy3d(h, dev, (void*)host, field % 3, true));
+  return PHONO_OK;
+}
+
+int phono_elem_size(const phono_handle* h) { return h ? h->es : fail(PHONO_ERR_ARG, "handle is NULL"); }
+
+int phono_energy(phono_handle* h, double out[2]) {
+  if (!h || !out) return fail(PHONO_ERR_ARG, "NULL argument");
+  EnergyArgs a{};
+  a.g = h->g;
+  a.ux = field_ptr(h, PHONO_FIELD_UX);
+  a.uy = field_ptr(h, PHONO_FIELD_UY);
+  a.uz = field_ptr(h, PHONO_FIELD_UZ);
+  const bool f64 = h->d.precision == PHONO_F64;
+  a.vx = field_ptr(h, f64 ? PHONO_FIELD_UX_OLD : PHONO_FIELD_VX);
+  a.vy = field_ptr(h, f64 ? PHONO_FIELD_UY_OLD : PHONO_FIELD_VY);
+  a.vz = field_ptr(h, f64 ? PHONO_FIELD_UZ_OLD : PHONO_FIELD_VZ);
+  a.f32 = f64 ? 0 : 1;
+  a.inv_dt = 1.0 / h->d.dt;
+  a.fdx = h->sp64[0];
+  a.fdy = h->sp64[1];
+  a.fdz = h->sp64[2];
+  a.sdx = h->sp64[3];
+  a.sdy = h->sp64[4];
+  a.sdz = h->sp64[5];
+  a.mat = h->mat;
+  a.tab = h->tab13;
+  CK(launch_energy(a, h->partial, kEnergyBlocks, h->energy_out, h->stream));
+  CK(cudaMemcpyAsync(out, h->energy_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return PHONO_OK;
+}
+
+int phono_reset(phono_handle* h) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  const size_t fb = h->field_elems * h->es;
+  const bool f64 = h->d.precision == PHONO_F64;
+  for (int r = 0; r < (f64 ? 3 : 2); r++)
+    for (int c = 0; c < 3; c++) {
+      CK(cudaMemsetAsync(h->u[r][c], 0, fb, h->stream));
+      if (!f64) {
+        CK(cudaMemsetAsync(h->v[r][c], 0, fb, h->stream));
+        CK(cudaMemsetAsync(h->c[r][c], 0, fb, h->stream));
+      }
+    }
+  if (h->surf) CK(cudaMemsetAsync(h->surf, 0, (size_t)h->nrec_cap * h->d.nx * h->d.ny * h->es, h->stream));
+  CK(cudaMemsetAsync(h->step_base, 0, sizeof(int) * 2, h->stream));
+  h->steps_done = 0;
+  return PHONO_OK;
+}
+
+int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table, int nmat) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  int rc = check_materials(h, mat, table, nmat);
+  if (rc) return rc;
+  return upload_materials(h, mat, table, nmat);
+}
+
+void* phono_stream(phono_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+void phono_destroy(phono_handle* h) { release(h); }
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// Energy reduction of an FDTD state (FP64 accumulation, deterministic order).
+//
+// E_kin = 1/2 sum rho v^2 over the displacement points the interior update
+// writes, E_str = 1/2 sum T . e over the stress points the reference computes
+// (normal stresses at nodes, shears at edges; simulation/base_solver.py:323-433)
+// with unit weights.  v is the half-step velocity: (u - u_old)/dt for the
+// leapfrog state, the stored v for the velocity form.  Used only to judge the
+// error of the FP32 path against the FP64 path; the reference has no energy.
+//
+// Pass 1 writes one partial pair per block into a scratch array; pass 2 sums
+// the partials in block order in one block, so the result does not depend on
+// scheduling.
+#include "fdtd_common.cuh"
+
+namespace phono {
+
+
+__device__ __forceinline__ double ld(const void* p, int f32, long long off) {
+  return f32 ? (double)__ldg((const float*)p + off) : __ldg((const double*)p + off);
+}
+
+constexpr int EN_THREADS = 256;
+
+__global__ void __launch_bounds__(EN_THREADS) energy_partial_kernel(EnergyArgs a, double2* __restrict__ partial) {
+  const Geo& g = a.g;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  double ek = 0.0, es = 0.0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    int k = (int)(q % g.nz);
+    long long r = q / g.nz;
+    int j = (int)(r % g.ny);
+    int i = (int)(r / g.ny);
+    long long off = g.o0 + (long long)i * g.sx + (long long)j * g.sy + k;
+    auto rho = [&](int ii, int jj, int kk) {
+      int m = a.mat[g.mo0 + (long long)ii * g.msx + (long long)jj * g.msy + kk];
+      return a.tab[m * 13 + 12];
+    };
+    auto C = [&](int ii, int jj, int kk, int e) {
+      int m = a.mat[g.mo0 + (long long)ii * g.msx + (long long)jj * g.msy + kk];
+      return a.tab[m * 13 + e];
+    };
+    auto U = [&](const void* p, int ii, int jj, int kk) {
+      return ld(p, a.f32, g.o0 + (long long)ii * g.sx + (long long)jj * g.sy + kk);
+    };
+    auto vel = [&](const void* u, const void* v) {
+      double x = ld(v, a.f32, off);
+      return a.f32 ? x : (ld(u, 0, off) - x) * a.inv_dt;
+    };
+    // kinetic energy at the interior displacement points
+    if (i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
+      double v = vel(a.ux, a.vx);
+      ek += 0.5 * rho(i + 1, j, k) * v * v;
+    }
+    if (i >= 1 && i <= g.nx - 2 && j <= g.ny - 2 && k <= g.nz - 2) {
+      double v = vel(a.uy, a.vy);
+      ek += 0.5 * rho(i, j + 1, k) * v * v;
+    }
+    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
+      double v = vel(a.uz, a.vz);
+      ek += 0.5 * rho(i, j, k + 1) * v * v;
+    }
+    // strain energy: normal stresses at interior nodes
+    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
+      double e1 = (U(a.ux, i, j, k) - U(a.ux, i - 1, j, k)) / a.sdx[i - 1];
+      double e2 = (U(a.uy, i, j, k) - U(a.uy, i, j - 1, k)) / a.sdy[j - 1];
+      double e3 = (U(a.uz, i, j, k) - U(a.uz, i, j, k - 1)) / a.sdz[k - 1];
+      double t1 = C(i, j, k, 0) * e1 + C(i, j, k, 1) * e2 + C(i, j, k, 2) * e3;
+      double t2 = C(i, j, k, 3) * e1 + C(i, j, k, 4) * e2 + C(i, j, k, 5) * e3;
+      double t3 = C(i, j, k, 6) * e1 + C(i, j, k, 7) * e2 + C(i, j, k, 8) * e3;
+      es += 0.5 * (t1 * e1 + t2 * e2 + t3 * e3);
+    }
+    // shears at edges
+    if (i >= 1 && i <= g.nx - 2 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
+      double gam = (U(a.uy, i, j, k + 1) - U(a.uy, i, j, k)) / a.fdz[k] +
+                   (U(a.uz, i, j + 1, k) - U(a.uz, i, j, k)) / a.fdy[j];
+      es += 0.5 * C(i, j + 1, k + 1, 9) * gam * gam;
+    }
+    if (i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
+      double gam = (U(a.ux, i, j, k + 1) - U(a.ux, i, j, k)) / a.fdz[k] +
+                   (U(a.uz, i + 1, j, k) - U(a.uz, i, j, k)) / a.fdx[i];
+      es += 0.5 * C(i + 1, j, k + 1, 10) * gam * gam;
+    }
+    if (i <= g.nx - 2 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
+      double gam = (U(a.ux, i, j + 1, k) - U(a.ux, i, j, k)) / a.fdy[j] +
+                   (U(a.uy, i + 1, j, k) - U(a.uy, i, j, k)) / a.fdx[i];
+      es += 0.5 * C(i + 1, j + 1, k, 11) * gam * gam;
+    }
+  }
+  __shared__ double sk[EN_THREADS], ss[EN_THREADS];
+  sk[threadIdx.x] = ek;
+  ss[threadIdx.x] = es;
+  __syncthreads();
+  for (int w = EN_THREADS / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sk[threadIdx.x] += sk[threadIdx.x + w];
+      ss[threadIdx.x] += ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = make_double2(sk[0], ss[0]);
+}
+
+__global__ void __launch_bounds__(EN_THREADS) energy_final_kernel(const double2* __restrict__ partial, int n,
+                                                                    double* __restrict__ out) {
+  __shared__ double sk[EN_THREADS], ss[EN_THREADS];
+  double ek = 0.0, es = 0.0;
+  for (int q = threadIdx.x; q < n; q += EN_THREADS) {
+    ek += partial[q].x;
+    es += partial[q].y;
+  }
+  sk[threadIdx.x] = ek;
+  ss[threadIdx.x] = es;
+  __syncthreads();
+  for (int w = EN_THREADS / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sk[threadIdx.x] += sk[threadIdx.x + w];
+      ss[threadIdx.x] += ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sk[0];
+    out[1] = ss[0];
+  }
+}
+
+// partial must hold nblocks double2 values; out two doubles (device)
+cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st) {
+  energy_partial_kernel<<<nblocks, EN_THREADS, 0, st>>>(a, partial);
+  energy_final_kernel<<<1, EN_THREADS, 0, st>>>(partial, nblocks, out);
+  return cudaGetLastError();
+}
+
+}  // namespace phono

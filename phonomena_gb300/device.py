@@ -1,0 +1,151 @@
+"""One simulation resident on the GPU, driven through the C ABI.
+
+``DeviceSimulation`` owns a ``phono_handle``: field buffers, material ids and
+table, spacing arrays, source samples and the surface-record buffer all live
+in device memory; ``step(n)`` enqueues n fused step launches (graph replays)
+on the handle's stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+
+def field_shape(nx, ny, nz, comp):
+    """Reference shape of a displacement component (simulation/grid.py:88-90)."""
+    return (nx - (comp == 0), ny - (comp == 1), nz - (comp == 2))
+
+
+class DeviceSimulation:
+    """Device-resident FDTD state behind ``phono_create`` / ``phono_step``.
+
+    spacing: dict with fdx, fdy, fdz (n-1) and sdx, sdy, sdz (n-2) arrays (SI).
+    mat: (nx, ny, nz) uint8 node material ids.  table: (nmat, 13) rows
+    C00 C01 C02 C10 C11 C12 C20 C21 C22 C33 C44 C55 rho.
+    """
+
+    def __init__(self, spacing, mat, table, dt, *, precision="f64", surface_mode="reference", bc="absorbing",
+                 source_mode="line", max_steps=0, record_every=0, tile_j=0, x_segment=0):
+        L = _lib.load()
+        self._L = L
+        self.mat = np.ascontiguousarray(mat, dtype=np.uint8)
+        if self.mat.ndim != 3:
+            raise ValueError("mat must be a 3-D (nx, ny, nz) array")
+        self.nx, self.ny, self.nz = map(int, self.mat.shape)
+        self._sp = {k: np.ascontiguousarray(np.ravel(spacing[k]), dtype=np.float64)
+                    for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")}
+        for k, n in (("fdx", self.nx - 1), ("fdy", self.ny - 1), ("fdz", self.nz - 1),
+                     ("sdx", self.nx - 2), ("sdy", self.ny - 2), ("sdz", self.nz - 2)):
+            if self._sp[k].size != n:
+                raise ValueError(f"{k} has {self._sp[k].size} values, expected {n}")
+        self.table = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 13)
+        self.dt = float(dt)
+        self.precision = precision
+        self.record_every = int(record_every)
+        self.max_steps = int(max_steps)
+        self.dtype = np.float64 if precision == "f64" else np.float32
+        d = _lib.PhonoDesc(
+            self.nx, self.ny, self.nz,
+            *(self._sp[k].ctypes.data for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")),
+            self.mat.ctypes.data, self.table.ctypes.data, self.table.shape[0], self.dt,
+            _lib.PRECISIONS[precision], _lib.SURFACE_MODES[surface_mode], _lib.BCS[bc],
+            _lib.SOURCE_MODES[source_mode], self.max_steps, self.record_every, int(tile_j), int(x_segment))
+        h = ctypes.c_void_p()
+        check(L.phono_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+
+    # -- control ----------------------------------------------------------
+    def set_source(self, samples):
+        s = np.ascontiguousarray(samples, dtype=np.float64)
+        check(self._L.phono_set_source(self._h, s.ctypes.data, s.size))
+
+    def step(self, n):
+        check(self._L.phono_step(self._h, int(n)))
+
+    def reset(self):
+        """Zero the state, records and step counter (materials and source kept)."""
+        check(self._L.phono_reset(self._h))
+
+    def set_materials(self, mat, table):
+        m = np.ascontiguousarray(mat, dtype=np.uint8)
+        if m.shape != (self.nx, self.ny, self.nz):
+            raise ValueError("material ids must match the mesh shape")
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 13)
+        check(self._L.phono_set_materials(self._h, m.ctypes.data, t.ctypes.data, t.shape[0]))
+        self.mat, self.table = m, t
+
+    @property
+    def stream_ptr(self):
+        """cudaStream_t of the handle (for CUDA events recorded by the caller)."""
+        return int(self._L.phono_stream(self._h) or 0)
+
+    def sync(self):
+        check(self._L.phono_sync(self._h))
+
+    @property
+    def steps_done(self):
+        return int(self._L.phono_steps_done(self._h))
+
+    def last_step_ms(self):
+        ms = ctypes.c_float()
+        check(self._L.phono_last_step_ms(self._h, ctypes.byref(ms)))
+        return float(ms.value)
+
+    # -- data ------------------------------------------------------------
+    @property
+    def n_records(self):
+        return self.max_steps // self.record_every if self.record_every > 0 else 0
+
+    def read_surface(self, first=0, count=None, out=None):
+        if count is None:
+            count = self.steps_done // self.record_every - first if self.record_every > 0 else 0
+        shape = (max(count, 0), self.nx, self.ny)
+        if out is None:
+            out = np.empty(shape, dtype=self.dtype)
+        elif out.shape != shape or out.dtype != self.dtype or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous {self.dtype.__name__} array of shape {shape}")
+        check(self._L.phono_read_surface(self._h, int(first), int(max(count, 0)), out.ctypes.data))
+        return out
+
+    def download(self, field, out=None):
+        f = _lib.FIELDS[field]
+        shape = field_shape(self.nx, self.ny, self.nz, f % 3)
+        if out is None:
+            out = np.empty(shape, dtype=self.dtype)
+        elif out.shape != shape or out.dtype != self.dtype or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous {self.dtype.__name__} array of shape {shape}")
+        check(self._L.phono_download(self._h, f, out.ctypes.data, out.nbytes))
+        return out
+
+    def upload(self, field, arr):
+        f = _lib.FIELDS[field]
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.shape != field_shape(self.nx, self.ny, self.nz, f % 3):
+            raise ValueError(f"{field} must have shape {field_shape(self.nx, self.ny, self.nz, f % 3)}")
+        check(self._L.phono_upload(self._h, f, a.ctypes.data, a.nbytes))
+
+    def energy(self):
+        out = np.zeros(2, np.float64)
+        check(self._L.phono_energy(self._h, out.ctypes.data))
+        return float(out[0]), float(out[1])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.phono_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,220 @@
+"""GPU parity: the fused sm_103a kernels against the reference and the oracle.
+
+F64 must reproduce the reference solver's outputs bit for bit (golden
+fixtures, produced by phonomena's own solver_default); F32K must reproduce the
+oracle's FP32 restatement bit for bit and stay within 1e-5 relative L2 of
+FP64.  All calls go through the C ABI (libphono_gpu.so via ctypes).
+"""
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+SURF = {"reference": 0, "corrected": 1}
+BC = {"absorbing": 0, "rigid": 1}
+
+
+def device_sim(d, precision="f64", steps=None, record_every=None, **kw):
+    from phonomena_gb300.device import DeviceSimulation
+
+    m = d["meta"]
+    steps = steps or m["steps"]
+    sim = DeviceSimulation(G.spacing(d), d["ids"], d["table"], d["dt"], precision=precision,
+                           surface_mode=m["surface_mode"], bc=m["bc"], source_mode=m["source_mode"],
+                           max_steps=len(d["src"]), record_every=m["record_every"] if record_every is None
+                           else record_every, **kw)
+    sim.set_source(d["src"])
+    return sim
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_f64_bit_exact_vs_reference(gpu_lib, name):
+    d = G.load(name)
+    with device_sim(d) as sim:
+        sim.step(d["meta"]["steps"])
+        sim.sync()
+        for key in ("ux", "uy", "uz"):
+            assert G.matches(d, key, sim.download(key)), f"{name}: {key} differs from the reference"
+        assert G.matches(d, "surf", sim.read_surface()), f"{name}: surface differs from the reference"
+
+
+@pytest.mark.parametrize("tile_j,x_segment", [(4, 5), (8, 64), (16, 3), (8, 1)])
+@pytest.mark.parametrize("name", ["small3_ref", "config1_void_corrected", "nonuniform_json"])
+def test_f64_tile_shapes_bit_exact(gpu_lib, name, tile_j, x_segment):
+    d = G.load(name)
+    with device_sim(d, tile_j=tile_j, x_segment=x_segment) as sim:
+        sim.step(d["meta"]["steps"])
+        sim.sync()
+        for key in ("ux", "uy", "uz"):
+            assert G.matches(d, key, sim.download(key)), f"{name} tj={tile_j} xs={x_segment}: {key}"
+
+
+def test_f64_split_calls_equal_one_run(gpu_lib):
+    """Graph replays (12-step chunks) and single launches interleave correctly."""
+    d = G.load("config1_void_corrected")
+    with device_sim(d) as sim:
+        for n in (5, 12, 1, 30, 24, 7, 421):
+            sim.step(n)
+        sim.sync()
+        assert sim.steps_done == 500
+        for key in ("ux", "uy", "uz"):
+            assert G.matches(d, key, sim.download(key))
+        assert G.matches(d, "surf", sim.read_surface())
+
+
+def _oracle_prob(oracle, d):
+    m = d["meta"]
+    return oracle.OracleProblem(G.spacing(d), d["ids"], d["table"], d["dt"], d["src"],
+                                surface_mode=SURF[m["surface_mode"]], bc=BC[m["bc"]])
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_f32k_bit_exact_vs_oracle(gpu_lib, oracle, name):
+    d = G.load(name)
+    m = d["meta"]
+    st, surf = oracle.run_f32k(_oracle_prob(oracle, d), record_every=m["record_every"])
+    with device_sim(d, precision="f32k") as sim:
+        sim.step(m["steps"])
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), st.u):
+            got = sim.download(key)
+            assert np.array_equal(got, ref), f"{name}: {key} max diff {np.abs(got - ref).max()}"
+        for key, ref in zip(("vx", "vy", "vz"), st.v):
+            assert np.array_equal(sim.download(key), ref), f"{name}: {key}"
+        for key, ref in zip(("cx", "cy", "cz"), st.c):
+            assert np.array_equal(sim.download(key), ref), f"{name}: {key}"
+        assert np.array_equal(sim.read_surface(), surf)
+
+
+def _crystal_case(cells, steps, seed, surface_mode="corrected"):
+    from phonomena_gb300 import crystal
+
+    spec = crystal.CrystalSpec(cells=cells, lattice=16, radius=(0.2, 0.4), depth=10, tungsten_frac=0.25,
+                               seed=seed, steps=steps)
+    g, m = crystal.build(spec)
+    src = crystal.sin_source(spec.freq, m.dt, steps)
+    d = dict(fdx=g.spacing()["fdx"], fdy=g.spacing()["fdy"], fdz=g.spacing()["fdz"], sdx=g.spacing()["sdx"],
+             sdy=g.spacing()["sdy"], sdz=g.spacing()["sdz"], ids=m.ids, table=m.table, dt=m.dt, src=src,
+             meta=dict(steps=steps, record_every=10, surface_mode=surface_mode, bc="absorbing", source_mode="line"))
+    return d
+
+
+@pytest.mark.parametrize("cells,tile_j", [((70, 45, 37), 8), ((33, 64, 65), 16), ((40, 40, 20), 4)])
+def test_f64_and_f32k_vs_oracle_multi_tile(gpu_lib, oracle, cells, tile_j):
+    """Grids with ragged tiles in y and z and several x segments."""
+    d = _crystal_case(cells, 60, seed=sum(cells))
+    prob = _oracle_prob(oracle, d)
+    s64, surf64 = oracle.run_f64(prob, record_every=10)
+    s32, surf32 = oracle.run_f32k(prob, record_every=10)
+    with device_sim(d, tile_j=tile_j, x_segment=16) as sim:
+        sim.step(60)
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), s64.u):
+            assert np.array_equal(sim.download(key), ref), key
+        assert np.array_equal(sim.read_surface(), surf64)
+    with device_sim(d, precision="f32k", tile_j=tile_j, x_segment=16) as sim:
+        sim.step(60)
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), s32.u):
+            assert np.array_equal(sim.download(key), ref), key
+        assert np.array_equal(sim.read_surface(), surf32)
+
+
+def test_wall_source_matches_oracle(gpu_lib, oracle):
+    d = G.load("small3_corrected")
+    m = d["meta"]
+    prob = oracle.OracleProblem(G.spacing(d), d["ids"], d["table"], d["dt"], d["src"], surface_mode=1, source_mode=1)
+    st, surf = oracle.run_f64(prob, record_every=m["record_every"])
+    from phonomena_gb300.device import DeviceSimulation
+
+    with DeviceSimulation(G.spacing(d), d["ids"], d["table"], d["dt"], surface_mode="corrected",
+                          source_mode="wall", max_steps=m["steps"], record_every=m["record_every"]) as sim:
+        sim.set_source(d["src"])
+        sim.step(m["steps"])
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), st.u):
+            assert np.array_equal(sim.download(key), ref)
+        assert np.array_equal(sim.read_surface(), surf)
+
+
+def test_upload_download_resume(gpu_lib):
+    """Checkpoint/resume: download state mid-run, upload into a fresh handle, continue."""
+    d = G.load("config1_void_corrected")
+    with device_sim(d) as a:
+        a.step(200)
+        a.sync()
+        snap = {k: a.download(k) for k in ("ux", "uy", "uz", "ux_old", "uy_old", "uz_old")}
+    with device_sim(d) as b:
+        # advance the step counter of b to 200 without touching its fields
+        b.step(200)
+        b.sync()
+        for k, v in snap.items():
+            b.upload(k, v)
+        b.step(300)
+        b.sync()
+        for key in ("ux", "uy", "uz"):
+            assert G.matches(d, key, b.download(key))
+
+
+def test_energy_matches_numpy(gpu_lib):
+    d = G.load("small3_corrected")
+    with device_sim(d) as sim:
+        sim.step(d["meta"]["steps"])
+        sim.sync()
+        ek, es = sim.energy()
+        ux, uy, uz = (sim.download(k) for k in ("ux", "uy", "uz"))
+        ox, oy, oz = (sim.download(k) for k in ("ux_old", "uy_old", "uz_old"))
+    nx, ny, nz = d["ids"].shape
+    rho = d["table"][d["ids"], 12]
+    dt = d["dt"]
+    ek_ref = 0.5 * (np.sum(rho[1:, 1:-1, :-1] * ((ux - ox)[:, 1:-1, :-1] / dt) ** 2)
+                    + np.sum(rho[1:-1, 1:, :-1] * ((uy - oy)[1:-1, :, :-1] / dt) ** 2)
+                    + np.sum(rho[1:-1, 1:-1, 1:] * ((uz - oz)[1:-1, 1:-1, :] / dt) ** 2))
+    assert abs(ek - ek_ref) <= 1e-9 * abs(ek_ref)
+    assert es > 0
+
+
+def test_numeric_guard_reports_nonfinite(gpu_lib):
+    from phonomena_gb300._lib import PhonoError
+
+    d = G.load("small3_ref")
+    with device_sim(d) as sim:
+        bad = np.zeros(sim.download("uz").shape)
+        bad[2, 2, 0] = np.inf
+        sim.upload("uz", bad)
+        sim.step(3)
+        with pytest.raises(PhonoError, match="PHONO_ERR_NUMERIC"):
+            sim.sync()
+
+
+def test_invalid_arguments_rejected(gpu_lib):
+    from phonomena_gb300._lib import PhonoError
+
+    d = G.load("small3_ref")
+    with pytest.raises(PhonoError, match="PHONO_ERR_ARG"):
+        device_sim(d, tile_j=5)
+    bad = dict(d)
+    bad["ids"] = d["ids"].copy()
+    bad["ids"][1, 1, 1] = 7
+    with pytest.raises(PhonoError, match="material id"):
+        device_sim(bad)
+    with device_sim(d) as sim:
+        with pytest.raises(PhonoError, match="source"):
+            sim.step(len(d["src"]) + 1)
+
+
+def test_plugin_solver_test_defaults(gpu_lib):
+    """Solver().test() runs the reference's TestDefaults; the result equals the golden."""
+    from phonomena_gb300.solver_gb300 import Solver
+
+    d = G.load("testdefaults_ricker")
+    s = Solver()
+    s.cfg["write_mode"] = "off"
+    s.cfg["record_every"] = 2
+    s.test()
+    for key in ("ux", "uy", "uz"):
+        assert G.matches(d, key, getattr(s.g, key))
+    assert G.matches(d, "surf", s.surface)
+    s.release()

@@ -1,0 +1,136 @@
+"""Host-side logic on CPU: input mirror, C-ABI exports, plugin discovery."""
+import importlib.util
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_testdefaults_mirror_matches_reference_inputs():
+    from phonomena_gb300.base import TestDefaults
+
+    d = G.load("testdefaults_ricker")
+    g, m = TestDefaults.make()
+    g.buildMesh()
+    g.update()
+    m.update()
+    for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz"):
+        assert np.array_equal(np.ravel(getattr(g, k)), d[k]), k
+    assert m.dt == d["dt"]
+    assert np.array_equal(np.unique(m.table, axis=0), d["table"])
+
+
+@pytest.mark.parametrize("name,seed,tungsten", [("config1_void_corrected", 0, False),
+                                                ("config1_tungsten_ref", 1, True)])
+def test_crystal_mirror_matches_reference_inputs(name, seed, tungsten):
+    from phonomena_gb300 import crystal
+
+    d = G.load(name)
+    spec = crystal.config1(seed=seed, holes_are_tungsten=tungsten)
+    g, m = crystal.build(spec)
+    for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz"):
+        assert np.array_equal(g.spacing()[k], d[k]), k
+    assert m.dt == d["dt"]
+    # same per-node constants (the reference table is sorted and unused rows dropped)
+    assert np.array_equal(m.table[m.ids], d["table"][d["ids"]])
+    assert np.array_equal(crystal.sin_source(spec.freq, m.dt, spec.steps), d["src"])
+
+
+def test_nonuniform_coordinates_give_reference_spacings():
+    from phonomena_gb300.model import Grid
+
+    d = G.load("nonuniform_json")
+    g = Grid()
+    g.SI_conversion = d["SI"]
+    g.set_coordinates(d["x"], d["y"], d["z"])
+    g.update()
+    for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz"):
+        assert np.array_equal(g.spacing()[k], d[k]), k
+
+
+def test_ids_from_CP_roundtrip():
+    from phonomena_gb300.model import ids_from_CP
+
+    rng = np.random.default_rng(3)
+    C = rng.normal(size=(3, 6, 6))
+    P = np.array([1.0, 2.0, 3.0])
+    ids = rng.integers(0, 3, size=(4, 5, 6))
+    ids2, table = ids_from_CP(C[ids], P[ids])
+    assert np.array_equal(table[ids2][..., 12], P[ids])
+    assert np.array_equal(table[ids2][..., 9], C[ids][..., 3, 3])
+
+
+def test_ricker_source_matches_reference_expression():
+    from phonomena_gb300 import crystal
+
+    d = G.load("testdefaults_ricker")
+    assert np.array_equal(crystal.ricker_source(100, d["dt"], 10), d["src"])
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "phono.h").read_text()
+    return sorted(set(re.findall(r"\b(phono_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    """Build libphono_gpu.so (nvcc cross-compiles without a GPU), load it, check exports."""
+    import ctypes
+
+    from phonomena_gb300 import _lib, build
+
+    lib = build.build()
+    L = ctypes.CDLL(str(lib))
+    declared = _declared_symbols()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(L, name), f"{name} declared in include/phono.h but not exported"
+    assert set(_lib.EXPORTS) >= set(declared)
+    L.phono_abi_version.restype = ctypes.c_int
+    assert L.phono_abi_version() == 1
+
+
+def test_plugin_is_discoverable_like_common_findSolvers(tmp_path, monkeypatch):
+    """Mimic phonomena/common.py:122-145: import simulation.solvers.<module>, read Solver().name."""
+    pkg = tmp_path / "simulation" / "solvers"
+    pkg.mkdir(parents=True)
+    (tmp_path / "simulation" / "__init__.py").write_text("")
+    (pkg / "__init__.py").write_text("")
+    (pkg / "solver_gb300.py").write_text("from phonomena_gb300.solver_gb300 import *  # noqa\n"
+                                         "from phonomena_gb300.solver_gb300 import Solver, cfg  # noqa\n")
+    monkeypatch.syspath_prepend(str(tmp_path))
+    for mod in [m for m in sys.modules if m == "simulation" or m.startswith("simulation.")]:
+        monkeypatch.delitem(sys.modules, mod)
+    mod = __import__("simulation.solvers.solver_gb300", fromlist=["Solver"])
+    s = getattr(mod, "Solver")()
+    assert s.name == "gb300"
+    assert {"wave", "wave_args", "write_mode", "precision", "record_every"} <= set(s.cfg)
+    import json
+    json.dumps(s.cfg)  # cfg stays JSON-serialisable (common.py:213-216)
+
+
+def test_output_npz_schema(tmp_path):
+    from types import SimpleNamespace
+
+    from phonomena_gb300.base import TestDefaults
+    from phonomena_gb300.output import read_results, write_results
+
+    g, m = TestDefaults.make()
+    g.update()
+    m.update()
+    nx, ny, nz = g.shape
+    g.ux, g.uy, g.uz = np.zeros((nx - 1, ny, nz)), np.zeros((nx, ny - 1, nz)), np.zeros((nx, ny, nz - 1))
+    s = SimpleNamespace(g=g, m=m, t=10, cfg={"wave": "ricker"}, record_every=2,
+                        surface=np.arange(5 * nx * ny, dtype=np.float64).reshape(5, nx, ny))
+    path = write_results(tmp_path / "out.hdf", s)
+    data, attrs = read_results(path)
+    assert data["uz"].shape == (nx, ny, 1, 5)
+    assert np.array_equal(data["uz"][:, :, 0, 3], s.surface[3])
+    assert attrs["dt_record"] == m.dt * 2
+    for k in ("x", "y", "z", "sdx", "fdz", "steps", "dt", "prim_material", "sec_material", "solver_cfg"):
+        assert k in attrs
