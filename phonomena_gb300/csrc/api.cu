@@ -604,7 +604,15 @@ int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
   int rc = check_materials(h, mat, table, nmat);
   if (rc) return rc;
-  return upload_materials(h, mat, table, nmat);
+  rc = upload_materials(h, mat, table, nmat);
+  if (rc) return rc;
+  // the absorbing-face coefficients are kernel arguments baked into the graph
+  if (h->graph) {
+    CK(cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return PHONO_OK;
 }
 
 void* phono_stream(phono_handle* h) { return h ? (void*)h->stream : nullptr; }
