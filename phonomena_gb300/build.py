@@ -21,7 +21,12 @@ LIB = BUILD / "libphono_gpu.so"
 SOURCES = ["fdtd_step.cu", "energy.cu", "api.cu"]
 HEADERS = ["fdtd_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# No implicit FMA anywhere: device code uses explicit _rn intrinsics for the
+# arithmetic whose rounding must match the reference, and the host code that
+# derives coefficients (api.cu) must round each operation like NumPy does; GCC
+# contracts a*b+c by default on aarch64, so -ffp-contract=off is required there.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

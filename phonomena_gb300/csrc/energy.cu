@@ -46,16 +46,16 @@ __global__ void __launch_bounds__(EN_THREADS) energy_partial_kernel(EnergyArgs a
       double x = ld(v, a.f32, off);
       return a.f32 ? x : (ld(u, 0, off) - x) * a.inv_dt;
     };
-    // kinetic energy at the interior displacement points
-    if (i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
+    // kinetic energy at the interior displacement points, absorbing faces excluded
+    if (i <= g.nx - 3 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
       double v = vel(a.ux, a.vx);
       ek += 0.5 * rho(i + 1, j, k) * v * v;
     }
-    if (i >= 1 && i <= g.nx - 2 && j <= g.ny - 2 && k <= g.nz - 2) {
+    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 3 && k <= g.nz - 2) {
       double v = vel(a.uy, a.vy);
       ek += 0.5 * rho(i, j + 1, k) * v * v;
     }
-    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
+    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 3) {
       double v = vel(a.uz, a.vz);
       ek += 0.5 * rho(i, j, k + 1) * v * v;
     }

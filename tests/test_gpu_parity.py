@@ -169,9 +169,10 @@ def test_energy_matches_numpy(gpu_lib):
     nx, ny, nz = d["ids"].shape
     rho = d["table"][d["ids"], 12]
     dt = d["dt"]
-    ek_ref = 0.5 * (np.sum(rho[1:, 1:-1, :-1] * ((ux - ox)[:, 1:-1, :-1] / dt) ** 2)
-                    + np.sum(rho[1:-1, 1:, :-1] * ((uy - oy)[1:-1, :, :-1] / dt) ** 2)
-                    + np.sum(rho[1:-1, 1:-1, 1:] * ((uz - oz)[1:-1, 1:-1, :] / dt) ** 2))
+    # interior points without the absorbing faces
+    ek_ref = 0.5 * (np.sum(rho[1:-1, 1:-1, :-1] * ((ux - ox)[:-1, 1:-1, :-1] / dt) ** 2)
+                    + np.sum(rho[1:-1, 2:-1, :-1] * ((uy - oy)[1:-1, 1:-1, :-1] / dt) ** 2)
+                    + np.sum(rho[1:-1, 1:-1, 1:-1] * ((uz - oz)[1:-1, 1:-1, :-1] / dt) ** 2))
     assert abs(ek - ek_ref) <= 1e-9 * abs(ek_ref)
     assert es > 0
 
