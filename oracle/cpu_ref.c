@@ -640,7 +640,9 @@ static void f32_faces(const ora_problem *p, const f32consts *K, const ora_f32k_s
     const float *ux = s->ux, *uy = s->uy, *uz = s->uz;
     float *xn = o->ux, *yn = o->uy, *zn = o->uz;
     const float *c = K->abc;
-#define F32ABC(dst, nbr_new, nbr_old, self_old, coef) (dst) = fmaf((coef), (nbr_new) - (self_old), (nbr_old))
+    const int rigid = p->bc == 1;
+#define F32ABC(dst, nbr_new, nbr_old, self_old, coef) \
+    (dst) = rigid ? 0.0f : fmaf((coef), (nbr_new) - (self_old), (nbr_old))
     for (int j = 0; j < ny; j++)
         for (int k = 0; k < nz; k++)
             F32ABC(xn[I3(ny, nz, nx - 2, j, k)], xn[I3(ny, nz, nx - 3, j, k)], ux[I3(ny, nz, nx - 3, j, k)],
