@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/phono.h"
+#include <cudaTypedefs.h>
 #include "fdtd_common.cuh"
 
 namespace phono {
@@ -43,9 +44,11 @@ struct phono_handle {
   size_t field_elems = 0;  // per array
   size_t mat_bytes = 0;
   std::vector<void*> allocs;
-  void* u[3][3] = {};
-  void* v[2][3] = {};
-  void* c[2][3] = {};
+  int nbuf = 3;            // u buffers: 3 rotating (F64) or 2 ping-pong (F32K)
+  char* ubase = nullptr;   // nbuf x 3 padded arrays, buffer-major
+  char* vbase = nullptr;   // F32K: 2 x 3 velocity arrays
+  char* cbase = nullptr;   // F32K: 2 x 3 Kahan arrays
+  CUtensorMap tm_u{}, tm_mat{};
   void* sp[6] = {};       // R spacings (F64 raw, F32K reciprocals)
   double* sp64[6] = {};   // raw double spacings (energy)
   double h_sp0[6] = {};   // first elements (raw)
@@ -189,14 +192,12 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.mat = h->mat;
   a.tab = (const R*)h->tab;
   a.src = h->src;
-  a.nsrc = h->nsrc;
-  for (int r = 0; r < 3; r++)
-    for (int c = 0; c < 3; c++) a.u[r][c] = (R*)h->u[r][c];
-  for (int r = 0; r < 2; r++)
-    for (int c = 0; c < 3; c++) {
-      a.v[r][c] = (R*)h->v[r][c];
-      a.c[r][c] = (R*)h->c[r][c];
-    }
+  a.tm_u = h->tm_u;
+  a.tm_mat = h->tm_mat;
+  a.nmat = h->nmat;
+  a.ubase = (R*)h->ubase;
+  a.vbase = (R*)h->vbase;
+  a.cbase = (R*)h->cbase;
   for (int q = 0; q < 8; q++) a.abc[q] = (R)h->abc[q];
   a.surf = (R*)h->surf;
   a.record_every = h->d.record_every;
@@ -275,20 +276,57 @@ static cudaError_t copy3d(phono_handle* h, void* dev, void* host, int c, bool to
 }
 
 // buffers holding the current state after steps_done steps
+static void* arr(const phono_handle* h, char* base, int buf, int comp) {
+  return base + (size_t)(buf * 3 + comp) * h->field_elems * h->es;
+}
+
 static void* field_ptr(phono_handle* h, int field) {
   int t = h->steps_done;
   int comp = field % 3;
   if (h->d.precision == PHONO_F64) {
-    if (field <= PHONO_FIELD_UZ) return h->u[(t + 1) % 3][comp];
-    if (field <= PHONO_FIELD_UZ_OLD) return h->u[t % 3][comp];
+    if (field <= PHONO_FIELD_UZ) return arr(h, h->ubase, (t + 1) % 3, comp);
+    if (field <= PHONO_FIELD_UZ_OLD) return arr(h, h->ubase, t % 3, comp);
     return nullptr;
   }
   int b = t & 1;
-  if (field <= PHONO_FIELD_UZ) return h->u[b][comp];
+  if (field <= PHONO_FIELD_UZ) return arr(h, h->ubase, b, comp);
   if (field <= PHONO_FIELD_UZ_OLD) return nullptr;
-  if (field <= PHONO_FIELD_VZ) return h->v[b][comp];
-  if (field <= PHONO_FIELD_CZ) return h->c[b][comp];
+  if (field <= PHONO_FIELD_VZ) return arr(h, h->vbase, b, comp);
+  if (field <= PHONO_FIELD_CZ) return arr(h, h->cbase, b, comp);
   return nullptr;
+}
+
+// TMA descriptors: a 4-D (k, j, i, array) map over the u allocation with a
+// (KW, TJ+2, 1, 3) box (one plane tile of the three components of a buffer)
+// and a 3-D (k, j, i) map over the material ids with a (48, TJ+2, 1) box.
+static int encode_tensor_maps(phono_handle* h) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn) return fail(PHONO_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const int es = h->es;
+  const int kw = es == 8 ? Lay<double>::KW : Lay<float>::KW;
+  cuuint64_t dims[4] = {(cuuint64_t)h->g.sy, (cuuint64_t)(h->d.ny + 2), (cuuint64_t)(h->d.nx + 2),
+                        (cuuint64_t)(h->nbuf * 3)};
+  cuuint64_t strides[3] = {(cuuint64_t)h->g.sy * es, (cuuint64_t)h->g.sx * es, (cuuint64_t)h->field_elems * es};
+  cuuint32_t box[4] = {(cuuint32_t)kw, (cuuint32_t)(h->tj + 2), 1, 3};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode(&h->tm_u, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                      h->ubase, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PHONO_ERR_CUDA, "cuTensorMapEncodeTiled (fields) failed: " + std::to_string(r));
+  cuuint64_t mdims[3] = {(cuuint64_t)h->g.msy, (cuuint64_t)(h->d.ny + 2), (cuuint64_t)(h->d.nx + 2)};
+  cuuint64_t mstr[2] = {(cuuint64_t)h->g.msy, (cuuint64_t)h->g.msx};
+  cuuint32_t mbox[3] = {(cuuint32_t)MKW, (cuuint32_t)(h->tj + 2), 1};
+  r = encode(&h->tm_mat, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, h->mat, mdims, mstr, mbox, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PHONO_ERR_CUDA, "cuTensorMapEncodeTiled (materials) failed: " + std::to_string(r));
+  return PHONO_OK;
 }
 
 extern "C" {
@@ -311,8 +349,9 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->es = f64 ? 8 : 4;
   const int nx = d->nx, ny = d->ny, nz = d->nz;
   // padded layout: planes -1..nx, rows -1..ny, 32-byte front pad in z
-  const long long koff = 32 / h->es;
+  const long long koff = f64 ? Lay<double>::KOFF : Lay<float>::KOFF;
   const long long pz = round_up(koff + nz + 1, 128 / h->es);
+  h->nbuf = f64 ? 3 : 2;
   h->g.nx = nx;
   h->g.ny = ny;
   h->g.nz = nz;
@@ -320,10 +359,11 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->g.sx = (long long)(ny + 2) * pz;
   h->g.o0 = h->g.sx + h->g.sy + koff;
   h->field_elems = (size_t)(nx + 2) * h->g.sx;
-  const long long mpz = round_up(nz + 2, 16);
+  h->g.fstride = (long long)h->field_elems;
+  const long long mpz = round_up(MKOFF + nz + 1, 16);
   h->g.msy = mpz;
   h->g.msx = (long long)(ny + 2) * mpz;
-  h->g.mo0 = h->g.msx + h->g.msy + 1;
+  h->g.mo0 = h->g.msx + h->g.msy + MKOFF;
   h->mat_bytes = (size_t)(nx + 2) * h->g.msx;
 
   // tiles
@@ -379,19 +419,15 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   TRYC(f64 ? configure_step_f64(h->tj) : configure_step_f32k(h->tj));
   TRYC(cudaEventCreate(&h->ev0));
   TRYC(cudaEventCreate(&h->ev1));
-  const size_t fb = h->field_elems * h->es;
-  if (f64) {
-    for (int r = 0; r < 3; r++)
-      for (int c = 0; c < 3; c++) TRY(dalloc(h, &h->u[r][c], fb));
-  } else {
-    for (int r = 0; r < 2; r++)
-      for (int c = 0; c < 3; c++) {
-        TRY(dalloc(h, &h->u[r][c], fb));
-        TRY(dalloc(h, &h->v[r][c], fb));
-        TRY(dalloc(h, &h->c[r][c], fb));
-      }
+  const size_t fb = h->field_elems * h->es * 3 * h->nbuf;
+  TRY(dalloc(h, (void**)&h->ubase, fb));
+  TRYC(cudaMemsetAsync(h->ubase, 0, fb, h->stream));
+  if (!f64) {
+    TRY(dalloc(h, (void**)&h->vbase, fb));
+    TRY(dalloc(h, (void**)&h->cbase, fb));
+    TRYC(cudaMemsetAsync(h->vbase, 0, fb, h->stream));
+    TRYC(cudaMemsetAsync(h->cbase, 0, fb, h->stream));
   }
-  for (void* p : h->allocs) TRYC(cudaMemsetAsync(p, 0, fb, h->stream));
 
   // spacings
   const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
@@ -416,6 +452,7 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   TRY(dalloc(h, &h->tab, (size_t)256 * 16 * h->es));
   TRY(dalloc(h, (void**)&h->tab13, (size_t)256 * PHONO_TABLE_COLS * 8));
   TRY(upload_materials(h, d->mat, d->table, d->nmat));
+  TRY(encode_tensor_maps(h));
   // source table, surface records, counters
   int cap = d->max_steps > 0 ? d->max_steps : 1;
   TRY(dalloc(h, (void**)&h->src, (size_t)cap * 8));
@@ -584,16 +621,10 @@ int phono_energy(phono_handle* h, double out[2]) {
 
 int phono_reset(phono_handle* h) {
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
-  const size_t fb = h->field_elems * h->es;
-  const bool f64 = h->d.precision == PHONO_F64;
-  for (int r = 0; r < (f64 ? 3 : 2); r++)
-    for (int c = 0; c < 3; c++) {
-      CK(cudaMemsetAsync(h->u[r][c], 0, fb, h->stream));
-      if (!f64) {
-        CK(cudaMemsetAsync(h->v[r][c], 0, fb, h->stream));
-        CK(cudaMemsetAsync(h->c[r][c], 0, fb, h->stream));
-      }
-    }
+  const size_t fb = h->field_elems * h->es * 3 * h->nbuf;
+  CK(cudaMemsetAsync(h->ubase, 0, fb, h->stream));
+  if (h->vbase) CK(cudaMemsetAsync(h->vbase, 0, fb, h->stream));
+  if (h->cbase) CK(cudaMemsetAsync(h->cbase, 0, fb, h->stream));
   if (h->surf) CK(cudaMemsetAsync(h->surf, 0, (size_t)h->nrec_cap * h->d.nx * h->d.ny * h->es, h->stream));
   CK(cudaMemsetAsync(h->step_base, 0, sizeof(int) * 2, h->stream));
   h->steps_done = 0;

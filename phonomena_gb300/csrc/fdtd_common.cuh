@@ -1,4 +1,4 @@
-// Shared device-side definitions of the fused elastic FDTD step.
+// Shared definitions of the fused elastic FDTD step (device and host side).
 //
 // Physics: phonomena's displacement-stress staggered-grid scheme
 // (simulation/base_solver.py:323-571).  The stresses T1..T6 are recomputed
@@ -7,26 +7,50 @@
 // point is a pure function of the input state and the kernel has no in-step
 // read/write hazards.
 //
-// Layout of every field array on the device (one array per component and
-// buffer; all three components share the padded extents):
+// Layout of the displacement fields on the device: one allocation holding
+// nbuf x 3 arrays (buffer-major, then component ux, uy, uz), each with the
+// padded extents
 //   element (i, j, k) at  o0 + i*sx + j*sy + k,   i in [-1, nx], j in [-1, ny],
-//   k in [-KOFF, pz-KOFF) with the (0,0,0) row start 32-byte aligned.
-// The padding layers are zero and never written, so the 1-node halo of every
+//   k in [-KOFF, sy-KOFF) with the (0,0,0) row start 32-byte aligned,
+// so that one 4-D TMA box (k, j, i, component) loads a plane tile of all three
+// components.  The padding is zero and never written: the 1-node halo of every
 // stencil read exists without bounds checks.  Component extents inside that
 // box follow the reference shapes (simulation/grid.py:88-110):
 //   ux (nx-1, ny, nz)   uy (nx, ny-1, nz)   uz (nx, ny, nz-1)
-// Material ids use the same (i, j, k) addressing with their own pitch.
+// Material ids (uint8) use the same (i, j, k) addressing with their own
+// pitch and an 8-byte front pad in k.
 #pragma once
+#include <cuda.h>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace phono {
 
-constexpr int TK = 32;  // tile width along z (the contiguous axis): one warp
+constexpr int TK = 32;      // tile width along z (the contiguous axis): one warp
+constexpr int NSLOT = 4;    // planes in the shared-memory ring
+constexpr int MKOFF = 8;    // material front pad in k (bytes)
+constexpr int MKW = 48;     // material tile width in k (bytes): k0-8 .. k0+40
+constexpr int TAB_SMEM = 32;  // material rows staged in shared memory
+
+template <class R>
+struct Lay;
+template <>
+struct Lay<double> {
+  static constexpr int KOFF = 4;   // field front pad in k (elements): 32 bytes
+  static constexpr int KW = 36;    // tile width in k: k0-2 .. k0+34 (288 bytes)
+  static constexpr int KB = 2;     // column of k0 inside the tile
+};
+template <>
+struct Lay<float> {
+  static constexpr int KOFF = 8;
+  static constexpr int KW = 40;    // k0-4 .. k0+36 (160 bytes)
+  static constexpr int KB = 4;
+};
 
 struct Geo {
   int nx, ny, nz;          // mesh nodes per axis
   long long sx, sy, o0;    // field strides (elements) and offset of (0,0,0)
+  long long fstride;       // elements between consecutive field arrays
   long long msx, msy, mo0; // material-id strides and offset
 };
 
@@ -41,24 +65,26 @@ struct Spacing {
 };
 
 // Face-point enumeration: for component c and plane p (0 z=N, 1 y=N, 2 y=0,
-// 3 x=N), faces_off[c*4+p] is the first flattened index; faces_off[12] is the
-// total.  Planes are disjoint (a point on several faces belongs to the first
-// plane in that order).
+// 3 x=N), off[c*4+p] is the first flattened index; off[12] is the total.
+// Planes are disjoint (a point on several faces belongs to the first plane in
+// that order).
 struct FaceTable {
   int off[13];
 };
 
 template <class R>
 struct StepArgs {
+  CUtensorMap tm_u;    // 4-D (k, j, i, buffer*3+component) map of the u allocation
+  CUtensorMap tm_mat;  // 3-D (k, j, i) map of the material ids
   Geo g;
   Spacing<R> sp;
   const uint8_t* __restrict__ mat;
-  const R* __restrict__ tab;   // 16 entries per material id
+  const R* __restrict__ tab;       // 16 entries per material id
+  int nmat;
   const double* __restrict__ src;  // source sample per global step
-  int nsrc;
-  R* u[3][3];    // F64: [rotation][component]; F32K: [buffer][component] (2 used)
-  R* v[2][3];    // F32K velocity; unused by F64
-  R* c[2][3];    // F32K Kahan compensation; unused by F64
+  R* ubase;      // u allocation: array (buffer*3 + c) at ubase + (buffer*3+c)*fstride
+  R* vbase;      // F32K velocity arrays (2 buffers x 3), same layout
+  R* cbase;      // F32K Kahan compensation arrays
   R abc[8];      // clx[-1] ctx[-1] cty[0] cly[0] cty[-1] cly[-1] ctz[-1] clz[-1]
   R* surf;       // surface records: [slot][nx][ny]
   int record_every;
@@ -71,7 +97,7 @@ struct StepArgs {
   int ntj, ntk, nseg, xseg;
   int n_tile_blocks;
   FaceTable faces;
-  int* __restrict__ err;  // device error flags (non-finite output etc.)
+  int* __restrict__ err;  // device error flags: 1 non-finite surface value, 2 pipeline wait timed out
 };
 
 // arguments of the energy reduction (energy.cu)

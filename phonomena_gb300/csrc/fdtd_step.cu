@@ -4,11 +4,15 @@
 // (simulation/base_solver.py:245-266).  The launch has two kinds of blocks:
 //
 //  * tile blocks: a (TJ x 32) tile of the (y, z) plane marches along x over a
-//    segment of planes.  Each iteration loads the next plane of u (3
-//    components, 1-node halo) into a 3-plane shared-memory ring, evaluates the
-//    six stresses of the current plane once (plus the halo stresses the
-//    neighbours need) into shared memory, and writes the new displacement of
-//    the plane.  Stresses are never written to global memory.
+//    segment of planes.  Planes of u (all three components, 1-node halo) and
+//    of the material ids stream into a 4-slot shared-memory ring through TMA
+//    (cp.async.bulk.tensor, completion on an mbarrier per slot), two planes
+//    ahead of the plane being computed.  Each iteration evaluates the six
+//    stresses of the current plane once (plus the halo stresses the
+//    neighbours need) into shared memory and writes the new displacement of
+//    the plane.  Stresses are never written to global memory; the pointwise
+//    state (u_old, or v and the Kahan term) is prefetched one plane ahead
+//    into registers.
 //
 //  * face blocks: one thread per point of the four absorbing faces
 //    (x=N, y=0, y=N, z=N; simulation/base_solver.py:540-554).  The reference
@@ -37,16 +41,9 @@ struct F64 {
   static constexpr bool kahan = false;
   __device__ __forceinline__ static R sub(R a, R b) { return __dsub_rn(a, b); }
   // normal stresses ((C0*d1)/a + (C1*d2)/b) + (C2*d3)/d   (base_solver.py:329-351)
-  __device__ __forceinline__ static void tn(const R* c, R d1, R d2, R d3, R a, R b, R d, R& T1, R& T2, R& T3,
-                                            bool want3) {
-    T1 = __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(__ldg(c + 0), d1), a), __ddiv_rn(__dmul_rn(__ldg(c + 1), d2), b)),
-                   __ddiv_rn(__dmul_rn(__ldg(c + 2), d3), d));
-    T2 = __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(__ldg(c + 3), d1), a), __ddiv_rn(__dmul_rn(__ldg(c + 4), d2), b)),
-                   __ddiv_rn(__dmul_rn(__ldg(c + 5), d3), d));
-    T3 = want3 ? __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(__ldg(c + 6), d1), a),
-                                     __ddiv_rn(__dmul_rn(__ldg(c + 7), d2), b)),
-                           __ddiv_rn(__dmul_rn(__ldg(c + 8), d3), d))
-               : 0.0;
+  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
+    return __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(c[0], d1), a), __ddiv_rn(__dmul_rn(c[1], d2), b)),
+                     __ddiv_rn(__dmul_rn(c[2], d3), d));
   }
   // shear stress C * (d1/a + d2/b)   (base_solver.py:353-372)
   __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
@@ -65,22 +62,15 @@ struct F64 {
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __dadd_rn(nbr_old, __dmul_rn(coef, __dsub_rn(nbr_new, self_old)));
   }
-  // (2u - u_old) + (dt^2/P) * div   (base_solver.py:441-443)
-  __device__ __forceinline__ static R leap(R u, R uold, R dt2p, R dv) {
-    return __dadd_rn(__dsub_rn(__dmul_rn(2.0, u), uold), __dmul_rn(dt2p, dv));
-  }
 };
 
 struct F32K {
   using R = float;
   static constexpr bool kahan = true;
   __device__ __forceinline__ static R sub(R a, R b) { return __fsub_rn(a, b); }
-  __device__ __forceinline__ static void tn(const R* c, R d1, R d2, R d3, R a, R b, R d, R& T1, R& T2, R& T3,
-                                            bool want3) {
-    R e1 = __fmul_rn(d1, a), e2 = __fmul_rn(d2, b), e3 = __fmul_rn(d3, d);
-    T1 = __fmaf_rn(__ldg(c + 0), e1, __fmaf_rn(__ldg(c + 1), e2, __fmul_rn(__ldg(c + 2), e3)));
-    T2 = __fmaf_rn(__ldg(c + 3), e1, __fmaf_rn(__ldg(c + 4), e2, __fmul_rn(__ldg(c + 5), e3)));
-    T3 = want3 ? __fmaf_rn(__ldg(c + 6), e1, __fmaf_rn(__ldg(c + 7), e2, __fmul_rn(__ldg(c + 8), e3))) : 0.0f;
+  // strains e = d * (1/spacing); T = fmaf(C0, e1, fmaf(C1, e2, C2 * e3))
+  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
+    return __fmaf_rn(c[0], __fmul_rn(d1, a), __fmaf_rn(c[1], __fmul_rn(d2, b), __fmul_rn(c[2], __fmul_rn(d3, d))));
   }
   __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
     return __fmul_rn(cs, __fmaf_rn(d1, a, __fmul_rn(d2, b)));
@@ -102,11 +92,6 @@ struct F32K {
 __device__ __forceinline__ long long fidx(const Geo& g, int i, int j, int k) {
   return g.o0 + (long long)i * g.sx + (long long)j * g.sy + k;
 }
-template <class R>
-__device__ __forceinline__ const R* mrow(const StepArgs<R>& a, int i, int j, int k) {
-  int m = __ldg(a.mat + a.g.mo0 + (long long)i * a.g.msx + (long long)j * a.g.msy + k);
-  return a.tab + m * 16;
-}
 
 // component extents and face coordinates
 __device__ __forceinline__ int ext_x(const Geo& g, int c) { return g.nx - (c == 0); }
@@ -124,9 +109,26 @@ __device__ __forceinline__ bool in_v0(const Geo& g, int c, int i, int j, int k) 
 }
 
 // ---------------------------------------------------------------------------
-// stress at a point, given a displacement fetcher F (x/y/z(i,j,k) -> R)
-// zero wherever the reference never writes the stress array
+// stress at a point, given a fetcher F: x/y/z(i,j,k) -> u, row(i,j,k) -> the
+// 16-entry material row.  Zero wherever the reference never writes the
+// stress array.
 // ---------------------------------------------------------------------------
+template <class S, class F>
+__device__ __forceinline__ typename S::R t1_at(const StepArgs<typename S::R>& a, const F& f, int i, int j, int k,
+                                               int which) {  // which: 0 T1, 1 T2, 2 T3
+  using R = typename S::R;
+  const Geo& g = a.g;
+  if (i < 1 || i > g.nx - 2 || j < 1 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
+  if (k == 0 && which == 2) return R(0);  // T3[1:-1,1:-1,0] = 0 (base_solver.py:418)
+  const R* c = f.row(i, j, k) + 3 * which;
+  R d1 = S::sub(f.x(i, j, k), f.x(i - 1, j, k));
+  R d2 = S::sub(f.y(i, j, k), f.y(i, j - 1, k));
+  if (k == 0)  // base_solver.py:408-416: uz - 0, first-element spacings
+    return S::tn1(c, d1, d2, f.z(i, j, 0), a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+  return S::tn1(c, d1, d2, S::sub(f.z(i, j, k), f.z(i, j, k - 1)), __ldg(a.sp.sdx + i - 1),
+                __ldg(a.sp.sdy + j - 1), __ldg(a.sp.sdz + k - 1));
+}
+
 template <class S, class F>
 __device__ __forceinline__ void t123_at(const StepArgs<typename S::R>& a, const F& f, int i, int j, int k,
                                         typename S::R& T1, typename S::R& T2, typename S::R& T3) {
@@ -136,16 +138,20 @@ __device__ __forceinline__ void t123_at(const StepArgs<typename S::R>& a, const 
     T1 = T2 = T3 = R(0);
     return;
   }
-  const R* c = mrow(a, i, j, k);
+  const R* c = f.row(i, j, k);
   R d1 = S::sub(f.x(i, j, k), f.x(i - 1, j, k));
   R d2 = S::sub(f.y(i, j, k), f.y(i, j - 1, k));
-  if (k == 0) {  // base_solver.py:408-418 (uz - 0, scalar spacings, T3 = 0)
+  if (k == 0) {
     R d3 = f.z(i, j, 0);
-    S::tn(c, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0, T1, T2, T3, false);
+    T1 = S::tn1(c, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+    T2 = S::tn1(c + 3, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+    T3 = R(0);
   } else {
     R d3 = S::sub(f.z(i, j, k), f.z(i, j, k - 1));
-    S::tn(c, d1, d2, d3, __ldg(a.sp.sdx + i - 1), __ldg(a.sp.sdy + j - 1), __ldg(a.sp.sdz + k - 1), T1, T2, T3,
-          true);
+    R sa = __ldg(a.sp.sdx + i - 1), sb = __ldg(a.sp.sdy + j - 1), sd = __ldg(a.sp.sdz + k - 1);
+    T1 = S::tn1(c, d1, d2, d3, sa, sb, sd);
+    T2 = S::tn1(c + 3, d1, d2, d3, sa, sb, sd);
+    T3 = S::tn1(c + 6, d1, d2, d3, sa, sb, sd);
   }
 }
 
@@ -155,9 +161,9 @@ __device__ __forceinline__ typename S::R t4_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 1 || i > g.nx - 2 || j < 0 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:420-423
-    return S::ts(__ldg(mrow(a, i, j + 1, 0) + 9), S::sub(f.y(i, j, 1), f.y(i, j, 0)), a.sp.fdy0,
+    return S::ts(f.row(i, j + 1, 0)[9], S::sub(f.y(i, j, 1), f.y(i, j, 0)), a.sp.fdy0,
                  S::sub(f.z(i, j + 1, 0), f.z(i, j, 0)), a.sp.fdz0);
-  return S::ts(__ldg(mrow(a, i, j + 1, k + 1) + 9), S::sub(f.y(i, j, k + 1), f.y(i, j, k)), __ldg(a.sp.fdz + k),
+  return S::ts(f.row(i, j + 1, k + 1)[9], S::sub(f.y(i, j, k + 1), f.y(i, j, k)), __ldg(a.sp.fdz + k),
                S::sub(f.z(i, j + 1, k), f.z(i, j, k)), __ldg(a.sp.fdy + j));
 }
 
@@ -167,9 +173,9 @@ __device__ __forceinline__ typename S::R t5_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 0 || i > g.nx - 2 || j < 1 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:425-428
-    return S::ts(__ldg(mrow(a, i + 1, j, 0) + 10), S::sub(f.x(i, j, 1), f.x(i, j, 0)), a.sp.fdx0,
+    return S::ts(f.row(i + 1, j, 0)[10], S::sub(f.x(i, j, 1), f.x(i, j, 0)), a.sp.fdx0,
                  S::sub(f.z(i + 1, j, 0), f.z(i, j, 0)), a.sp.fdz0);
-  return S::ts(__ldg(mrow(a, i + 1, j, k + 1) + 10), S::sub(f.x(i, j, k + 1), f.x(i, j, k)), __ldg(a.sp.fdz + k),
+  return S::ts(f.row(i + 1, j, k + 1)[10], S::sub(f.x(i, j, k + 1), f.x(i, j, k)), __ldg(a.sp.fdz + k),
                S::sub(f.z(i + 1, j, k), f.z(i, j, k)), __ldg(a.sp.fdx + i));
 }
 
@@ -179,126 +185,147 @@ __device__ __forceinline__ typename S::R t6_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 0 || i > g.nx - 2 || j < 0 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:430-433
-    return S::ts(__ldg(mrow(a, i + 1, j + 1, 0) + 11), S::sub(f.x(i, j + 1, 0), f.x(i, j, 0)), a.sp.fdx0,
+    return S::ts(f.row(i + 1, j + 1, 0)[11], S::sub(f.x(i, j + 1, 0), f.x(i, j, 0)), a.sp.fdx0,
                  S::sub(f.y(i + 1, j, 0), f.y(i, j, 0)), a.sp.fdz0);
-  return S::ts(__ldg(mrow(a, i + 1, j + 1, k) + 11), S::sub(f.x(i, j + 1, k), f.x(i, j, k)), __ldg(a.sp.fdy + j),
+  return S::ts(f.row(i + 1, j + 1, k)[11], S::sub(f.x(i, j + 1, k), f.x(i, j, k)), __ldg(a.sp.fdy + j),
                S::sub(f.y(i + 1, j, k), f.y(i, j, k)), __ldg(a.sp.fdx + i));
 }
 
 // divergence terms of the three components (base_solver.py:441-463,495-516)
 // and the material row whose density applies
-template <class S>
-__device__ __forceinline__ typename S::R div_x(const StepArgs<typename S::R>& a, int i, int j, int k,
+template <class S, class F>
+__device__ __forceinline__ typename S::R div_x(const StepArgs<typename S::R>& a, const F& f, int i, int j, int k,
                                                typename S::R t1p, typename S::R t1m, typename S::R t6a,
                                                typename S::R t6b, typename S::R t5a, typename S::R t5b,
                                                const typename S::R*& row) {
   if (k == 0) {
-    row = mrow(a, i + 1, j, 0);
+    row = f.row(i + 1, j, 0);
     return S::div3(S::sub(t1p, t1m), a.sp.fdx0, S::sub(t6a, t6b), a.sp.sdy0, t5a, a.sp.sdz0);
   }
-  row = mrow(a, i + 1, j, k);
+  row = f.row(i + 1, j, k);
   return S::div3(S::sub(t1p, t1m), __ldg(a.sp.fdx + i), S::sub(t6a, t6b), __ldg(a.sp.sdy + j - 1),
                  S::sub(t5a, t5b), __ldg(a.sp.sdz + k - 1));
 }
-template <class S>
-__device__ __forceinline__ typename S::R div_y(const StepArgs<typename S::R>& a, int i, int j, int k,
+template <class S, class F>
+__device__ __forceinline__ typename S::R div_y(const StepArgs<typename S::R>& a, const F& f, int i, int j, int k,
                                                typename S::R t6a, typename S::R t6b, typename S::R t2p,
                                                typename S::R t2m, typename S::R t4a, typename S::R t4b,
                                                const typename S::R*& row) {
   if (k == 0) {
-    row = mrow(a, i, j + 1, 0);
+    row = f.row(i, j + 1, 0);
     return S::div3(S::sub(t6a, t6b), a.sp.sdx0, S::sub(t2p, t2m), a.sp.fdy0, t4a, a.sp.sdz0);
   }
-  row = mrow(a, i, j + 1, k);
+  row = f.row(i, j + 1, k);
   return S::div3(S::sub(t6a, t6b), __ldg(a.sp.sdx + i - 1), S::sub(t2p, t2m), __ldg(a.sp.fdy + j),
                  S::sub(t4a, t4b), __ldg(a.sp.sdz + k - 1));
 }
-template <class S>
-__device__ __forceinline__ typename S::R div_z(const StepArgs<typename S::R>& a, int i, int j, int k,
+template <class S, class F>
+__device__ __forceinline__ typename S::R div_z(const StepArgs<typename S::R>& a, const F& f, int i, int j, int k,
                                                typename S::R t5a, typename S::R t5b, typename S::R t4a,
                                                typename S::R t4b, typename S::R t3p, typename S::R t3m,
                                                const typename S::R*& row) {
   if (k == 0) {
-    row = mrow(a, i, j, 0);  // density at z index 0 (base_solver.py:513)
+    row = f.row(i, j, 0);  // density at z index 0 (base_solver.py:513)
     if (a.surface_mode == 0) return S::div_surf_ref(S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p);
     return S::div3(S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p, a.sp.fdz0);
   }
-  row = mrow(a, i, j, k + 1);
+  row = f.row(i, j, k + 1);
   return S::div3(S::sub(t5a, t5b), __ldg(a.sp.sdx + i - 1), S::sub(t4a, t4b), __ldg(a.sp.sdy + j - 1),
                  S::sub(t3p, t3m), __ldg(a.sp.fdz + k));
 }
 
-// state roles of global step tt
+// state arrays of global step tt: buffer indices, pointers formed on use
+// (no pointer arrays, which would live in local memory)
 template <class R>
 struct Roles {
-  const R* cur[3];  // u at step tt (before the source overwrite)
-  const R* old[3];  // F64: u at tt-1
-  R* out[3];        // u at tt+1
-  const R* vin[3];
-  const R* cin[3];
-  R* vout[3];
-  R* cout[3];
+  R* ubase;
+  R* vbase;
+  R* cbase;
+  long long fs;
+  int rold, rcur, rout;  // buffer indices: u at tt-1 (F64), tt, tt+1
+  __device__ __forceinline__ const R* cur(int c) const { return ubase + (rcur * 3 + c) * fs; }
+  __device__ __forceinline__ const R* old(int c) const { return ubase + (rold * 3 + c) * fs; }
+  __device__ __forceinline__ R* out(int c) const { return ubase + (rout * 3 + c) * fs; }
+  __device__ __forceinline__ const R* vin(int c) const { return vbase + (rcur * 3 + c) * fs; }
+  __device__ __forceinline__ const R* cin(int c) const { return cbase + (rcur * 3 + c) * fs; }
+  __device__ __forceinline__ R* vout(int c) const { return vbase + (rout * 3 + c) * fs; }
+  __device__ __forceinline__ R* cout(int c) const { return cbase + (rout * 3 + c) * fs; }
 };
 
 template <class S>
 __device__ __forceinline__ Roles<typename S::R> roles(const StepArgs<typename S::R>& a, int tt) {
   Roles<typename S::R> r;
+  r.ubase = a.ubase;
+  r.vbase = a.vbase;
+  r.cbase = a.cbase;
+  r.fs = a.g.fstride;
   if (!S::kahan) {
-    int ro = tt % 3, rc = (tt + 1) % 3, rn = (tt + 2) % 3;
-    for (int c = 0; c < 3; c++) {
-      r.old[c] = a.u[ro][c];
-      r.cur[c] = a.u[rc][c];
-      r.out[c] = a.u[rn][c];
-      r.vin[c] = r.cin[c] = nullptr;
-      r.vout[c] = r.cout[c] = nullptr;
-    }
+    r.rold = tt % 3;
+    r.rcur = (tt + 1) % 3;
+    r.rout = (tt + 2) % 3;
   } else {
-    int bi = tt & 1, bo = bi ^ 1;
-    for (int c = 0; c < 3; c++) {
-      r.cur[c] = a.u[bi][c];
-      r.old[c] = nullptr;
-      r.out[c] = a.u[bo][c];
-      r.vin[c] = a.v[bi][c];
-      r.cin[c] = a.c[bi][c];
-      r.vout[c] = a.v[bo][c];
-      r.cout[c] = a.c[bo][c];
-    }
+    r.rcur = tt & 1;
+    r.rout = r.rcur ^ 1;
+    r.rold = r.rcur;
   }
   return r;
 }
 
-// new state of one V0 point: F64 leapfrog / F32K Kahan velocity update;
-// returns the new u and stores it (plus v, c)
+// pointwise state of a V0 point that the update needs besides u itself
+template <class R>
+struct Pw {
+  R p0, p1;  // F64: u_old, -; F32K: v, c
+};
+
 template <class S>
-__device__ __forceinline__ typename S::R update_point(const StepArgs<typename S::R>& a,
-                                                      const Roles<typename S::R>& r, int c, long long off,
-                                                      typename S::R u, typename S::R dv,
-                                                      const typename S::R* row, bool store) {
+__device__ __forceinline__ Pw<typename S::R> load_pw(const Roles<typename S::R>& r, int c, long long off) {
+  Pw<typename S::R> p;
+  if constexpr (!S::kahan) {
+    p.p0 = __ldg(r.old(c) + off);
+    p.p1 = 0;
+  } else {
+    p.p0 = __ldg(r.vin(c) + off);
+    p.p1 = __ldg(r.cin(c) + off);
+  }
+  return p;
+}
+
+// new state of one V0 point: F64 leapfrog / F32K Kahan velocity update
+template <class S>
+__device__ __forceinline__ typename S::R update_value(typename S::R u, Pw<typename S::R> pw, typename S::R dv,
+                                                      const typename S::R* row, typename S::R& vn,
+                                                      typename S::R& cn) {
   using R = typename S::R;
   if constexpr (!S::kahan) {
-    R un = S::leap(u, __ldg(r.old[c] + off), __ldg(row + 12), dv);
-    if (store) r.out[c][off] = un;
-    return un;
+    // (2u - u_old) + (dt^2/P) * div   (base_solver.py:441-443)
+    vn = cn = 0;
+    return __dadd_rn(__dsub_rn(__dmul_rn(2.0, u), pw.p0), __dmul_rn(row[12], dv));
   } else {
-    R v = __ldg(r.vin[c] + off), cm = __ldg(r.cin[c] + off);
-    R vn = __fmaf_rn(__ldg(row + 12), dv, v);
-    R y = __fmaf_rn(__ldg(row + 14), vn, -cm);  // row[14] = dt
+    R v2 = __fmaf_rn(row[12], dv, pw.p0);         // row[12] = dt / P
+    R y = __fmaf_rn(row[14], v2, -pw.p1);          // row[14] = dt
     R t = __fadd_rn(u, y);
-    if (store) {
-      r.cout[c][off] = __fsub_rn(__fsub_rn(t, u), y);
-      r.vout[c][off] = vn;
-      r.out[c][off] = t;
-    }
+    cn = __fsub_rn(__fsub_rn(t, u), y);
+    vn = v2;
     return t;
   }
 }
 
 template <class S>
-__device__ __forceinline__ void store_stale(const Roles<typename S::R>& r, int c, long long off) {
-  r.out[c][off] = __ldg(r.cur[c] + off);
+__device__ __forceinline__ void store_point(const Roles<typename S::R>& r, int c, long long off, typename S::R un,
+                                            typename S::R vn, typename S::R cn) {
+  r.out(c)[off] = un;
   if constexpr (S::kahan) {
-    r.vout[c][off] = __ldg(r.vin[c] + off);
-    r.cout[c][off] = __ldg(r.cin[c] + off);
+    r.vout(c)[off] = vn;
+    r.cout(c)[off] = cn;
+  }
+}
+
+template <class S>
+__device__ __forceinline__ void store_stale(const Roles<typename S::R>& r, int c, long long off) {
+  r.out(c)[off] = __ldg(r.cur(c) + off);
+  if constexpr (S::kahan) {
+    r.vout(c)[off] = __ldg(r.vin(c) + off);
+    r.cout(c)[off] = __ldg(r.cin(c) + off);
   }
 }
 
@@ -319,6 +346,8 @@ struct GlobalFetch {
   const R* ux;
   const R* uy;
   const R* uz;
+  const uint8_t* mat;
+  const R* tab;
   Geo g;
   R s;
   int wall;
@@ -328,19 +357,31 @@ struct GlobalFetch {
     if (i == 0 && (wall || k == 0)) return s;  // source overwrite (base_solver.py:251)
     return __ldg(uz + fidx(g, i, j, k));
   }
+  __device__ __forceinline__ const R* row(int i, int j, int k) const {
+    return tab + 16 * __ldg(mat + g.mo0 + (long long)i * g.msx + (long long)j * g.msy + k);
+  }
 };
 
 template <class R, int TJ>
 struct TileFetch {
-  static constexpr int W = TK + 2, PL = W * (TJ + 2);
-  const R* su;  // [3 slots][3 comps][PL]
-  int j0, k0;
+  static constexpr int KW = Lay<R>::KW, KB = Lay<R>::KB;
+  static constexpr int CW = (TJ + 2) * KW;                       // component stride in a slot
+  static constexpr int SU = ((3 * CW * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);  // slot stride
+  static constexpr int SM = (((TJ + 2) * MKW + 127) / 128) * 128;                               // mat slot stride
+  const R* uring;
+  const uint8_t* mring;
+  const R* tab;
+  int j0, k0, ibase;
+  __device__ __forceinline__ int slot(int i) const { return (i - ibase) & (NSLOT - 1); }
   __device__ __forceinline__ int loc(int i, int j, int k) const {
-    return (((i + 3) % 3) * 3) * PL + (j - j0 + 1) * W + (k - k0 + 1);
+    return slot(i) * SU + (j - j0 + 1) * KW + (k - k0 + KB);
   }
-  __device__ __forceinline__ R x(int i, int j, int k) const { return su[loc(i, j, k)]; }
-  __device__ __forceinline__ R y(int i, int j, int k) const { return su[loc(i, j, k) + PL]; }
-  __device__ __forceinline__ R z(int i, int j, int k) const { return su[loc(i, j, k) + 2 * PL]; }
+  __device__ __forceinline__ R x(int i, int j, int k) const { return uring[loc(i, j, k)]; }
+  __device__ __forceinline__ R y(int i, int j, int k) const { return uring[loc(i, j, k) + CW]; }
+  __device__ __forceinline__ R z(int i, int j, int k) const { return uring[loc(i, j, k) + 2 * CW]; }
+  __device__ __forceinline__ const R* row(int i, int j, int k) const {
+    return tab + 16 * mring[slot(i) * SM + (j - j0 + 1) * MKW + (k - k0 + MKOFF)];
+  }
 };
 
 // interior (V0) value of u_new at a point, evaluated from global memory
@@ -350,32 +391,24 @@ __device__ typename S::R v0_global(const StepArgs<typename S::R>& a, const Roles
   using R = typename S::R;
   const Geo& g = a.g;
   long long off = fidx(g, i, j, k);
-  if (!in_v0(g, c, i, j, k)) return __ldg(r.cur[c] + off);  // u_new not written this step: last value
+  if (!in_v0(g, c, i, j, k)) return __ldg(r.cur(c) + off);  // u_new not written this step: last value
   const R* row;
   R dv, u;
   if (c == 0) {
-    R t1p, t1m, d0, d1;
-    t123_at<S>(a, f, i + 1, j, k, t1p, d0, d1);
-    t123_at<S>(a, f, i, j, k, t1m, d0, d1);
-    dv = div_x<S>(a, i, j, k, t1p, t1m, t6_at<S>(a, f, i, j, k), t6_at<S>(a, f, i, j - 1, k),
-                  t5_at<S>(a, f, i, j, k), t5_at<S>(a, f, i, j, k - 1), row);
+    dv = div_x<S>(a, f, i, j, k, t1_at<S>(a, f, i + 1, j, k, 0), t1_at<S>(a, f, i, j, k, 0), t6_at<S>(a, f, i, j, k),
+                  t6_at<S>(a, f, i, j - 1, k), t5_at<S>(a, f, i, j, k), t5_at<S>(a, f, i, j, k - 1), row);
     u = f.x(i, j, k);
   } else if (c == 1) {
-    R t2p, t2m, d0, d1;
-    t123_at<S>(a, f, i, j + 1, k, d0, t2p, d1);
-    t123_at<S>(a, f, i, j, k, d0, t2m, d1);
-    dv = div_y<S>(a, i, j, k, t6_at<S>(a, f, i, j, k), t6_at<S>(a, f, i - 1, j, k), t2p, t2m,
-                  t4_at<S>(a, f, i, j, k), t4_at<S>(a, f, i, j, k - 1), row);
+    dv = div_y<S>(a, f, i, j, k, t6_at<S>(a, f, i, j, k), t6_at<S>(a, f, i - 1, j, k), t1_at<S>(a, f, i, j + 1, k, 1),
+                  t1_at<S>(a, f, i, j, k, 1), t4_at<S>(a, f, i, j, k), t4_at<S>(a, f, i, j, k - 1), row);
     u = f.y(i, j, k);
   } else {
-    R t3p, t3m, d0, d1;
-    t123_at<S>(a, f, i, j, k + 1, d0, d1, t3p);
-    t123_at<S>(a, f, i, j, k, d0, d1, t3m);
-    dv = div_z<S>(a, i, j, k, t5_at<S>(a, f, i, j, k), t5_at<S>(a, f, i - 1, j, k), t4_at<S>(a, f, i, j, k),
-                  t4_at<S>(a, f, i, j - 1, k), t3p, t3m, row);
+    dv = div_z<S>(a, f, i, j, k, t5_at<S>(a, f, i, j, k), t5_at<S>(a, f, i - 1, j, k), t4_at<S>(a, f, i, j, k),
+                  t4_at<S>(a, f, i, j - 1, k), t1_at<S>(a, f, i, j, k + 1, 2), t1_at<S>(a, f, i, j, k, 2), row);
     u = f.z(i, j, k);
   }
-  return update_point<S>(a, r, c, off, u, dv, row, false);
+  R vn, cn;
+  return update_value<S>(u, load_pw<S>(r, c, off), dv, row, vn, cn);
 }
 
 // final value of a face point: walk z=N, y=N, y=0, x=N (reverse of the
@@ -386,46 +419,99 @@ __device__ typename S::R face_value(const StepArgs<typename S::R>& a, const Role
   using R = typename S::R;
   const Geo& g = a.g;
   const int xi = ext_x(g, c) - 1, jN = ext_y(g, c) - 1, kz = ext_z(g, c) - 1;
-  int st[4], pi[4], pj[4], pk[4], n = 0;
   int ci = i, cj = j, ck = k;
-  if (ck == kz) { st[n] = 3; pi[n] = ci; pj[n] = cj; pk[n] = ck; n++; ck -= 1; }
-  if (cj == jN) { st[n] = 2; pi[n] = ci; pj[n] = cj; pk[n] = ck; n++; cj -= 1; }
-  if (cj == 0)  { st[n] = 1; pi[n] = ci; pj[n] = cj; pk[n] = ck; n++; cj += 1; }
-  if (ci == xi) { st[n] = 0; pi[n] = ci; pj[n] = cj; pk[n] = ck; n++; ci -= 1; }
-  R val = v0_global<S>(a, r, f, c, ci, cj, ck);
+  const bool sz = ck == kz;  // z = N face at (i, j, kz)
+  if (sz) ck -= 1;
+  const bool syn = cj == jN;  // y = N face at (i, jN, ck)
+  const int kyn = ck;
+  if (syn) cj -= 1;
+  const bool sy0 = cj == 0;  // y = 0 face at (i, 0, ck)
+  if (sy0) cj += 1;
+  const bool sx = ci == xi;  // x = N face at (xi, cj, ck)
+  if (sx) ci -= 1;
   auto U = [&](int ii, int jj, int kk) -> R {
     return c == 0 ? f.x(ii, jj, kk) : (c == 1 ? f.y(ii, jj, kk) : f.z(ii, jj, kk));
   };
-  for (int q = n - 1; q >= 0; q--) {
-    int bi = pi[q], bj = pj[q], bk = pk[q];
-    R coef;
-    int ni = bi, nj = bj, nk = bk;
-    switch (st[q]) {
-      case 0: coef = c == 0 ? a.abc[0] : a.abc[1]; ni = bi - 1; break;      // x = N: clx / ctx
-      case 1: coef = c == 1 ? a.abc[3] : a.abc[2]; nj = bj + 1; break;      // y = 0: cly / cty
-      case 2: coef = c == 1 ? a.abc[5] : a.abc[4]; nj = bj - 1; break;      // y = N
-      default: coef = c == 2 ? a.abc[7] : a.abc[6]; nk = bk - 1; break;     // z = N: clz / ctz
-    }
-    val = S::abc(coef, val, U(bi, bj, bk), U(ni, nj, nk));
-  }
+  R val = v0_global<S>(a, r, f, c, ci, cj, ck);
+  if (sx) val = S::abc(c == 0 ? a.abc[0] : a.abc[1], val, U(xi, cj, ck), U(xi - 1, cj, ck));
+  if (sy0) val = S::abc(c == 1 ? a.abc[3] : a.abc[2], val, U(i, 0, kyn), U(i, 1, kyn));
+  if (syn) val = S::abc(c == 1 ? a.abc[5] : a.abc[4], val, U(i, jN, kyn), U(i, jN - 1, kyn));
+  if (sz) val = S::abc(c == 2 ? a.abc[7] : a.abc[6], val, U(i, j, kz), U(i, j, kz - 1));
   return val;
 }
+
+// ---------------------------------------------------------------------------
+// TMA + mbarrier helpers (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false if the phase did not complete within the poll budget
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); it++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <class R, int TJ>
+struct SmemPlan {
+  using TF = TileFetch<R, TJ>;
+  static constexpr int W = TK + 2, PL = W * (TJ + 2);
+  static constexpr size_t BARS = 128;
+  static constexpr size_t TAB = TAB_SMEM * 16 * sizeof(R);
+  static constexpr size_t UR = (size_t)NSLOT * TF::SU * sizeof(R);
+  static constexpr size_t MR = (size_t)NSLOT * TF::SM;
+  static constexpr size_t TS = ((7 * PL * sizeof(R) + 127) / 128) * 128;
+  static constexpr size_t off_tab = BARS, off_u = off_tab + TAB, off_m = off_u + UR, off_t = off_m + MR;
+  static constexpr size_t total = off_t + TS + 128;  // + alignment slack
+  static constexpr uint32_t tx_bytes = (uint32_t)(3 * (TJ + 2) * Lay<R>::KW * sizeof(R) + (TJ + 2) * MKW);
+};
 
 // ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typename S::R> a) {
+__global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
+  using P = SmemPlan<R, TJ>;
+  using TF = TileFetch<R, TJ>;
   constexpr int NT = TK * TJ;
-  constexpr int W = TK + 2, PL = W * (TJ + 2);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R* su = reinterpret_cast<R*>(smem_raw);  // [3][3][PL]
-  R* sT2 = su + 9 * PL;
-  R* sT3 = sT2 + PL;
-  R* sT4 = sT3 + PL;
-  R* sT5 = sT4 + PL;  // [2][PL]
-  R* sT6 = sT5 + 2 * PL;  // [2][PL]
+  constexpr int W = P::W, PL = P::PL;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
 
   const Geo& g = a.g;
   const int tt = __ldg(a.step_base) + a.step_off;
@@ -446,19 +532,25 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
     else if (pl == 1) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = ey - 1; }
     else if (pl == 2) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = 0; }
     else { j = rr / (ez - 1); k = rr - j * (ez - 1); j += 1; i = ex - 1; }
-    GlobalFetch<R> f{r.cur[0], r.cur[1], r.cur[2], g, s, a.source_mode};
+    GlobalFetch<R> f{r.cur(0), r.cur(1), r.cur(2), a.mat, a.tab, g, s, a.source_mode};
     R val = a.bc == 1 ? R(0) : face_value<S>(a, r, f, c, i, j, k);
     long long off = fidx(g, i, j, k);
-    r.out[c][off] = val;
-    if constexpr (S::kahan) {
-      r.vout[c][off] = R(0);
-      r.cout[c][off] = R(0);
-    }
+    store_point<S>(r, c, off, val, R(0), R(0));
     if (c == 2 && k == 0) record(a, tt, i, j, val);
     return;
   }
 
   // ---------------- tile blocks ----------------
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base);
+  R* stab = reinterpret_cast<R*>(base + P::off_tab);
+  R* uring = reinterpret_cast<R*>(base + P::off_u);
+  uint8_t* mring = reinterpret_cast<uint8_t*>(base + P::off_m);
+  R* sT2 = reinterpret_cast<R*>(base + P::off_t);
+  R* sT3 = sT2 + PL;
+  R* sT4 = sT3 + PL;
+  R* sT5 = sT4 + PL;      // [2][PL]
+  R* sT6 = sT5 + 2 * PL;  // [2][PL]
+
   const int b = blockIdx.x;
   const int kt = b % a.ntk;
   const int rest = b / a.ntk;
@@ -467,41 +559,76 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
   const int j0 = jt * TJ, k0 = kt * TK;
   const int ib = seg * a.xseg;
   const int ie = min(ib + a.xseg, g.nx - 1);
+  const int ibase = ib - 1;
+  const int plast = ie + 1;  // last plane the segment reads
   const int j = j0 + threadIdx.y, k = k0 + threadIdx.x;
   const bool active = (j < g.ny - 1) && (k < g.nz - 1);
   const int L = (threadIdx.y + 1) * W + threadIdx.x + 1;
-  TileFetch<R, TJ> f{su, j0, k0};
 
-  auto load_plane = [&](int i) {
-    R* dst = su + ((i + 3) % 3) * 3 * PL;
-    const bool iv = (i >= -1 && i <= g.nx);
-    for (int qq = tid; qq < PL; qq += NT) {
-      int rr = qq / W, cc = qq - rr * W;
-      int gj = j0 - 1 + rr, gk = k0 - 1 + cc;
-      R vx = 0, vy = 0, vz = 0;
-      if (iv && gj <= g.ny && gk <= g.nz) {
-        long long off = fidx(g, i, gj, gk);
-        vx = __ldg(r.cur[0] + off);
-        vy = __ldg(r.cur[1] + off);
-        vz = (i == 0 && (a.source_mode == 1 || gk == 0)) ? s : __ldg(r.cur[2] + off);
-      }
-      dst[qq] = vx;
-      dst[qq + PL] = vy;
-      dst[qq + 2 * PL] = vz;
-    }
+  const bool tab_in_smem = a.nmat <= TAB_SMEM;
+  if (tab_in_smem)
+    for (int q = tid; q < a.nmat * 16; q += NT) stab[q] = __ldg(a.tab + q);
+  TF f{uring, mring, tab_in_smem ? stab : a.tab, j0, k0, ibase};
+
+  auto issue = [&](int p) {  // plane p into its ring slot (one thread)
+    const int q = p - ibase, sl = q & (NSLOT - 1);
+    mbar_expect_tx(&bars[sl], P::tx_bytes);
+    // padded coordinates: k + KOFF, j + 1, i + 1; the tiles start at k0-KB, j0-1
+    tma_load_4d(uring + sl * TF::SU, &a.tm_u, k0 - Lay<R>::KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
+    tma_load_3d(mring + sl * TF::SM, &a.tm_mat, k0, j0, p + 1, &bars[sl]);
+  };
+  bool ok = true;
+  auto wait_plane = [&](int p) {
+    const int q = p - ibase;
+    if (!mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1)) ok = false;
   };
 
-  // prologue: planes ib-1, ib; own T5, T6 at ib-1
-  load_plane(ib - 1);
-  load_plane(ib);
+  if (tid == 0) {
+    for (int q = 0; q < NSLOT; q++) mbar_init(&bars[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int issued = ibase - 1;  // last plane issued (thread 0)
+  if (tid == 0)
+    for (int p = ibase; p <= min(ibase + NSLOT - 1, plast); p++) {
+      issue(p);
+      issued = p;
+    }
+
+  // prologue: planes ib-1 and ib; source patch; own T5, T6 at ib-1
+  wait_plane(ib - 1);
+  wait_plane(ib);
+  if (ib == 0) {
+    R* zt = uring + f.slot(0) * TF::SU + 2 * TF::CW;
+    if (a.source_mode == 1) {
+      for (int q = tid; q < TF::CW; q += NT) zt[q] = s;
+    } else if (k0 == 0) {
+      for (int q = tid; q < TJ + 2; q += NT) zt[q * TF::KW + TF::KB] = s;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   __syncthreads();
   R t5m = t5_at<S>(a, f, ib - 1, j, k);
   R t6m = t6_at<S>(a, f, ib - 1, j, k);
   R t1m = 0, uxm = 0;
 
+  // pointwise state prefetch, one plane ahead: ux at plane i-1, uy/uz at plane i
+  auto want_y = [&](int i) { return active && i < ie && !on_face(g, 1, i, j, k) && in_v0(g, 1, i, j, k); };
+  auto want_z = [&](int i) { return active && i < ie && !on_face(g, 2, i, j, k) && in_v0(g, 2, i, j, k); };
+  auto want_x = [&](int i) {
+    return active && i > ib && i - 1 < ie && !on_face(g, 0, i - 1, j, k) && in_v0(g, 0, i - 1, j, k);
+  };
+  Pw<R> pwx{0, 0}, pwy{0, 0}, pwz{0, 0};
+  if (want_y(ib)) pwy = load_pw<S>(r, 1, fidx(g, ib, j, k));
+  if (want_z(ib)) pwz = load_pw<S>(r, 2, fidx(g, ib, j, k));
+
   for (int i = ib; i <= ie; i++) {
-    load_plane(i + 1);
-    __syncthreads();
+    Pw<R> nx_{0, 0}, ny_{0, 0}, nz_{0, 0};
+    if (want_x(i + 1)) nx_ = load_pw<S>(r, 0, fidx(g, i, j, k));
+    if (want_y(i + 1)) ny_ = load_pw<S>(r, 1, fidx(g, i + 1, j, k));
+    if (want_z(i + 1)) nz_ = load_pw<S>(r, 2, fidx(g, i + 1, j, k));
+    wait_plane(i + 1);
+    if (__syncthreads_or(!ok)) break;
     const int p = i & 1;
     // own stresses at plane i
     R t1c, t2c, t3c;
@@ -518,42 +645,38 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
     // T3 column k0+TK, T4/T5 column k0-1
     for (int qq = tid; qq < 3 * TK + 3 * TJ; qq += NT) {
       if (qq < TK) {
-        int kk = k0 + qq;
-        R d0, d1, t2;
-        t123_at<S>(a, f, i, j0 + TJ, kk, d0, t2, d1);
-        sT2[(TJ + 1) * W + qq + 1] = t2;
+        sT2[(TJ + 1) * W + qq + 1] = t1_at<S>(a, f, i, j0 + TJ, k0 + qq, 1);
       } else if (qq < 2 * TK) {
-        int kk = k0 + qq - TK;
-        sT6[p * PL + (qq - TK) + 1] = t6_at<S>(a, f, i, j0 - 1, kk);
+        sT6[p * PL + (qq - TK) + 1] = t6_at<S>(a, f, i, j0 - 1, k0 + qq - TK);
       } else if (qq < 3 * TK) {
-        int kk = k0 + qq - 2 * TK;
-        sT4[(qq - 2 * TK) + 1] = t4_at<S>(a, f, i, j0 - 1, kk);
+        sT4[(qq - 2 * TK) + 1] = t4_at<S>(a, f, i, j0 - 1, k0 + qq - 2 * TK);
       } else {
-        int w = qq - 3 * TK;
-        int which = w / TJ, jl = w - which * TJ;
-        int jj = j0 + jl;
-        if (which == 0) {
-          R d0, d1, t3;
-          t123_at<S>(a, f, i, jj, k0 + TK, d0, d1, t3);
-          sT3[(jl + 1) * W + TK + 1] = t3;
-        } else if (which == 1) {
-          sT4[(jl + 1) * W] = t4_at<S>(a, f, i, jj, k0 - 1);
-        } else {
-          sT5[p * PL + (jl + 1) * W] = t5_at<S>(a, f, i, jj, k0 - 1);
-        }
+        const int w = qq - 3 * TK;
+        const int which = w / TJ, jl = w - which * TJ;
+        const int jj = j0 + jl;
+        if (which == 0) sT3[(jl + 1) * W + TK + 1] = t1_at<S>(a, f, i, jj, k0 + TK, 2);
+        else if (which == 1) sT4[(jl + 1) * W] = t4_at<S>(a, f, i, jj, k0 - 1);
+        else sT5[p * PL + (jl + 1) * W] = t5_at<S>(a, f, i, jj, k0 - 1);
       }
     }
     const R uxc = f.x(i, j, k), uyc = f.y(i, j, k), uzc = f.z(i, j, k);
     __syncthreads();
+    // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
+    if (tid == 0 && i - 1 + NSLOT <= plast) {
+      issue(i - 1 + NSLOT);
+      issued = i - 1 + NSLOT;
+    }
     if (active) {
       if (i < ie) {
+        const long long off = fidx(g, i, j, k);
         // uy_new(i, j, k)
-        long long off = fidx(g, i, j, k);
         if (!on_face(g, 1, i, j, k)) {
           if (in_v0(g, 1, i, j, k)) {
             const R* row;
-            R dv = div_y<S>(a, i, j, k, t6c, t6m, sT2[L + W], t2c, t4c, sT4[L - 1], row);
-            update_point<S>(a, r, 1, off, uyc, dv, row, true);
+            R dv = div_y<S>(a, f, i, j, k, t6c, t6m, sT2[L + W], t2c, t4c, sT4[L - 1], row);
+            R vn, cn;
+            R un = update_value<S>(uyc, pwy, dv, row, vn, cn);
+            store_point<S>(r, 1, off, un, vn, cn);
           } else {
             store_stale<S>(r, 1, off);
           }
@@ -563,11 +686,13 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
           R val;
           if (in_v0(g, 2, i, j, k)) {
             const R* row;
-            R dv = div_z<S>(a, i, j, k, t5c, t5m, t4c, sT4[L - W], sT3[L + 1], t3c, row);
-            val = update_point<S>(a, r, 2, off, uzc, dv, row, true);
+            R dv = div_z<S>(a, f, i, j, k, t5c, t5m, t4c, sT4[L - W], sT3[L + 1], t3c, row);
+            R vn, cn;
+            val = update_value<S>(uzc, pwz, dv, row, vn, cn);
+            store_point<S>(r, 2, off, val, vn, cn);
           } else {
             store_stale<S>(r, 2, off);
-            val = __ldg(r.cur[2] + off);
+            val = __ldg(r.cur(2) + off);
           }
           if (k == 0) record(a, tt, i, j, val);
         }
@@ -575,14 +700,16 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
       if (i > ib) {
         // ux_new(i-1, j, k)
         const int im = i - 1;
-        long long off = fidx(g, im, j, k);
+        const long long off = fidx(g, im, j, k);
         if (!on_face(g, 0, im, j, k)) {
           if (in_v0(g, 0, im, j, k)) {
             const int pm = p ^ 1;
             const R* row;
-            R dv = div_x<S>(a, im, j, k, t1c, t1m, sT6[pm * PL + L], sT6[pm * PL + L - W], sT5[pm * PL + L],
+            R dv = div_x<S>(a, f, im, j, k, t1c, t1m, sT6[pm * PL + L], sT6[pm * PL + L - W], sT5[pm * PL + L],
                             sT5[pm * PL + L - 1], row);
-            update_point<S>(a, r, 0, off, uxm, dv, row, true);
+            R vn, cn;
+            R un = update_value<S>(uxm, pwx, dv, row, vn, cn);
+            store_point<S>(r, 0, off, un, vn, cn);
           } else {
             store_stale<S>(r, 0, off);
           }
@@ -593,6 +720,20 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
     t5m = t5c;
     t6m = t6c;
     uxm = uxc;
+    pwx = nx_;
+    pwy = ny_;
+    pwz = nz_;
+  }
+  if (!ok) {
+    // a pipeline wait ran out: flag it and drain the copies this block issued
+    if (tid == 0) {
+      atomicOr(a.err, 2);
+      for (int p = max(ibase, issued - NSLOT + 1); p <= issued; p++) {
+        const int q = p - ibase;
+        mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -601,14 +742,18 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const StepArgs<typen
 // ---------------------------------------------------------------------------
 template <class R>
 size_t step_smem_bytes(int tj) {
-  int PL = (TK + 2) * (tj + 2);
-  return sizeof(R) * (size_t)PL * (9 + 3 + 4);
+  switch (tj) {
+    case 4: return SmemPlan<R, 4>::total;
+    case 8: return SmemPlan<R, 8>::total;
+    case 16: return SmemPlan<R, 16>::total;
+    default: return 0;
+  }
 }
 
 template <class S, int TJ>
 static cudaError_t configure_tj() {
   return cudaFuncSetAttribute(fdtd_step_kernel<S, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)step_smem_bytes<typename S::R>(TJ));
+                              (int)SmemPlan<typename S::R, TJ>::total);
 }
 
 template <class S>
@@ -625,7 +770,7 @@ template <class S, int TJ>
 static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int n_face_blocks, cudaStream_t st) {
   dim3 block(TK, TJ);
   dim3 grid(a.n_tile_blocks + n_face_blocks);
-  fdtd_step_kernel<S, TJ><<<grid, block, step_smem_bytes<typename S::R>(TJ), st>>>(a);
+  fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<typename S::R, TJ>::total, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -639,17 +784,7 @@ cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int n_face_blo
   }
 }
 
-template cudaError_t configure_step<F64>(int);
-template cudaError_t configure_step<F32K>(int);
-template cudaError_t launch_step<F64>(const StepArgs<double>&, int, int, cudaStream_t);
-template cudaError_t launch_step<F32K>(const StepArgs<float>&, int, int, cudaStream_t);
-template size_t step_smem_bytes<double>(int);
-template size_t step_smem_bytes<float>(int);
-
-}  // namespace phono
-
 // non-template entry points for the C ABI translation unit
-namespace phono {
 cudaError_t configure_step_f64(int tj) { return configure_step<F64>(tj); }
 cudaError_t configure_step_f32k(int tj) { return configure_step<F32K>(tj); }
 cudaError_t launch_step_f64(const StepArgs<double>& a, int tj, int nf, cudaStream_t st) {
@@ -658,4 +793,5 @@ cudaError_t launch_step_f64(const StepArgs<double>& a, int tj, int nf, cudaStrea
 cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int nf, cudaStream_t st) {
   return launch_step<F32K>(a, tj, nf, st);
 }
+
 }  // namespace phono
