@@ -595,10 +595,11 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const __grid_constan
       issued = p;
     }
 
-  // prologue: planes ib-1 and ib; source patch; own T5, T6 at ib-1
+  // prologue: planes ib-1 and ib; source patch (plane 0 is in the ring when
+  // it is plane ib or ib-1); own T5, T6 at ib-1
   wait_plane(ib - 1);
   wait_plane(ib);
-  if (ib == 0) {
+  if (ib <= 1) {
     R* zt = uring + f.slot(0) * TF::SU + 2 * TF::CW;
     if (a.source_mode == 1) {
       for (int q = tid; q < TF::CW; q += NT) zt[q] = s;
