@@ -500,11 +500,14 @@ struct SmemPlan {
   static constexpr uint32_t tx_bytes = (uint32_t)(3 * (TJ + 2) * Lay<R>::KW * sizeof(R) + (TJ + 2) * MKW);
 };
 
+#include "tile_path.cuh"
+
 // ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
+// FP32: 32 resident warps per SM (64 registers, no spills); FP64: unconstrained
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
+__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : 1)) fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
   using P = SmemPlan<R, TJ>;
   using TF = TileFetch<R, TJ>;
@@ -541,201 +544,7 @@ __global__ void __launch_bounds__(TK * TJ) fdtd_step_kernel(const __grid_constan
   }
 
   // ---------------- tile blocks ----------------
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base);
-  R* stab = reinterpret_cast<R*>(base + P::off_tab);
-  R* uring = reinterpret_cast<R*>(base + P::off_u);
-  uint8_t* mring = reinterpret_cast<uint8_t*>(base + P::off_m);
-  R* sT2 = reinterpret_cast<R*>(base + P::off_t);
-  R* sT3 = sT2 + PL;
-  R* sT4 = sT3 + PL;
-  R* sT5 = sT4 + PL;      // [2][PL]
-  R* sT6 = sT5 + 2 * PL;  // [2][PL]
-
-  const int b = blockIdx.x;
-  const int kt = b % a.ntk;
-  const int rest = b / a.ntk;
-  const int jt = rest % a.ntj;
-  const int seg = rest / a.ntj;
-  const int j0 = jt * TJ, k0 = kt * TK;
-  const int ib = seg * a.xseg;
-  const int ie = min(ib + a.xseg, g.nx - 1);
-  const int ibase = ib - 1;
-  const int plast = ie + 1;  // last plane the segment reads
-  const int j = j0 + threadIdx.y, k = k0 + threadIdx.x;
-  const bool active = (j < g.ny - 1) && (k < g.nz - 1);
-  const int L = (threadIdx.y + 1) * W + threadIdx.x + 1;
-
-  const bool tab_in_smem = a.nmat <= TAB_SMEM;
-  if (tab_in_smem)
-    for (int q = tid; q < a.nmat * 16; q += NT) stab[q] = __ldg(a.tab + q);
-  TF f{uring, mring, tab_in_smem ? stab : a.tab, j0, k0, ibase};
-
-  auto issue = [&](int p) {  // plane p into its ring slot (one thread)
-    const int q = p - ibase, sl = q & (NSLOT - 1);
-    mbar_expect_tx(&bars[sl], P::tx_bytes);
-    // padded coordinates: k + KOFF, j + 1, i + 1; the tiles start at k0-KB, j0-1
-    tma_load_4d(uring + sl * TF::SU, &a.tm_u, k0 - Lay<R>::KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
-    tma_load_3d(mring + sl * TF::SM, &a.tm_mat, k0, j0, p + 1, &bars[sl]);
-  };
-  bool ok = true;
-  auto wait_plane = [&](int p) {
-    const int q = p - ibase;
-    if (!mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1)) ok = false;
-  };
-
-  if (tid == 0) {
-    for (int q = 0; q < NSLOT; q++) mbar_init(&bars[q], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  int issued = ibase - 1;  // last plane issued (thread 0)
-  if (tid == 0)
-    for (int p = ibase; p <= min(ibase + NSLOT - 1, plast); p++) {
-      issue(p);
-      issued = p;
-    }
-
-  // prologue: planes ib-1 and ib; source patch (plane 0 is in the ring when
-  // it is plane ib or ib-1); own T5, T6 at ib-1
-  wait_plane(ib - 1);
-  wait_plane(ib);
-  if (ib <= 1) {
-    R* zt = uring + f.slot(0) * TF::SU + 2 * TF::CW;
-    if (a.source_mode == 1) {
-      for (int q = tid; q < TF::CW; q += NT) zt[q] = s;
-    } else if (k0 == 0) {
-      for (int q = tid; q < TJ + 2; q += NT) zt[q * TF::KW + TF::KB] = s;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  R t5m = t5_at<S>(a, f, ib - 1, j, k);
-  R t6m = t6_at<S>(a, f, ib - 1, j, k);
-  R t1m = 0, uxm = 0;
-
-  // pointwise state prefetch, one plane ahead: ux at plane i-1, uy/uz at plane i
-  auto want_y = [&](int i) { return active && i < ie && !on_face(g, 1, i, j, k) && in_v0(g, 1, i, j, k); };
-  auto want_z = [&](int i) { return active && i < ie && !on_face(g, 2, i, j, k) && in_v0(g, 2, i, j, k); };
-  auto want_x = [&](int i) {
-    return active && i > ib && i - 1 < ie && !on_face(g, 0, i - 1, j, k) && in_v0(g, 0, i - 1, j, k);
-  };
-  Pw<R> pwx{0, 0}, pwy{0, 0}, pwz{0, 0};
-  if (want_y(ib)) pwy = load_pw<S>(r, 1, fidx(g, ib, j, k));
-  if (want_z(ib)) pwz = load_pw<S>(r, 2, fidx(g, ib, j, k));
-
-  for (int i = ib; i <= ie; i++) {
-    Pw<R> nx_{0, 0}, ny_{0, 0}, nz_{0, 0};
-    if (want_x(i + 1)) nx_ = load_pw<S>(r, 0, fidx(g, i, j, k));
-    if (want_y(i + 1)) ny_ = load_pw<S>(r, 1, fidx(g, i + 1, j, k));
-    if (want_z(i + 1)) nz_ = load_pw<S>(r, 2, fidx(g, i + 1, j, k));
-    wait_plane(i + 1);
-    if (__syncthreads_or(!ok)) break;
-    const int p = i & 1;
-    // own stresses at plane i
-    R t1c, t2c, t3c;
-    t123_at<S>(a, f, i, j, k, t1c, t2c, t3c);
-    R t4c = t4_at<S>(a, f, i, j, k);
-    R t5c = t5_at<S>(a, f, i, j, k);
-    R t6c = t6_at<S>(a, f, i, j, k);
-    sT2[L] = t2c;
-    sT3[L] = t3c;
-    sT4[L] = t4c;
-    sT5[p * PL + L] = t5c;
-    sT6[p * PL + L] = t6c;
-    // halo stresses the neighbours need: T2 row j0+TJ, T6/T4 row j0-1,
-    // T3 column k0+TK, T4/T5 column k0-1
-    for (int qq = tid; qq < 3 * TK + 3 * TJ; qq += NT) {
-      if (qq < TK) {
-        sT2[(TJ + 1) * W + qq + 1] = t1_at<S>(a, f, i, j0 + TJ, k0 + qq, 1);
-      } else if (qq < 2 * TK) {
-        sT6[p * PL + (qq - TK) + 1] = t6_at<S>(a, f, i, j0 - 1, k0 + qq - TK);
-      } else if (qq < 3 * TK) {
-        sT4[(qq - 2 * TK) + 1] = t4_at<S>(a, f, i, j0 - 1, k0 + qq - 2 * TK);
-      } else {
-        const int w = qq - 3 * TK;
-        const int which = w / TJ, jl = w - which * TJ;
-        const int jj = j0 + jl;
-        if (which == 0) sT3[(jl + 1) * W + TK + 1] = t1_at<S>(a, f, i, jj, k0 + TK, 2);
-        else if (which == 1) sT4[(jl + 1) * W] = t4_at<S>(a, f, i, jj, k0 - 1);
-        else sT5[p * PL + (jl + 1) * W] = t5_at<S>(a, f, i, jj, k0 - 1);
-      }
-    }
-    const R uxc = f.x(i, j, k), uyc = f.y(i, j, k), uzc = f.z(i, j, k);
-    __syncthreads();
-    // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
-    if (tid == 0 && i - 1 + NSLOT <= plast) {
-      issue(i - 1 + NSLOT);
-      issued = i - 1 + NSLOT;
-    }
-    if (active) {
-      if (i < ie) {
-        const long long off = fidx(g, i, j, k);
-        // uy_new(i, j, k)
-        if (!on_face(g, 1, i, j, k)) {
-          if (in_v0(g, 1, i, j, k)) {
-            const R* row;
-            R dv = div_y<S>(a, f, i, j, k, t6c, t6m, sT2[L + W], t2c, t4c, sT4[L - 1], row);
-            R vn, cn;
-            R un = update_value<S>(uyc, pwy, dv, row, vn, cn);
-            store_point<S>(r, 1, off, un, vn, cn);
-          } else {
-            store_stale<S>(r, 1, off);
-          }
-        }
-        // uz_new(i, j, k)
-        if (!on_face(g, 2, i, j, k)) {
-          R val;
-          if (in_v0(g, 2, i, j, k)) {
-            const R* row;
-            R dv = div_z<S>(a, f, i, j, k, t5c, t5m, t4c, sT4[L - W], sT3[L + 1], t3c, row);
-            R vn, cn;
-            val = update_value<S>(uzc, pwz, dv, row, vn, cn);
-            store_point<S>(r, 2, off, val, vn, cn);
-          } else {
-            store_stale<S>(r, 2, off);
-            val = __ldg(r.cur(2) + off);
-          }
-          if (k == 0) record(a, tt, i, j, val);
-        }
-      }
-      if (i > ib) {
-        // ux_new(i-1, j, k)
-        const int im = i - 1;
-        const long long off = fidx(g, im, j, k);
-        if (!on_face(g, 0, im, j, k)) {
-          if (in_v0(g, 0, im, j, k)) {
-            const int pm = p ^ 1;
-            const R* row;
-            R dv = div_x<S>(a, f, im, j, k, t1c, t1m, sT6[pm * PL + L], sT6[pm * PL + L - W], sT5[pm * PL + L],
-                            sT5[pm * PL + L - 1], row);
-            R vn, cn;
-            R un = update_value<S>(uxm, pwx, dv, row, vn, cn);
-            store_point<S>(r, 0, off, un, vn, cn);
-          } else {
-            store_stale<S>(r, 0, off);
-          }
-        }
-      }
-    }
-    t1m = t1c;
-    t5m = t5c;
-    t6m = t6c;
-    uxm = uxc;
-    pwx = nx_;
-    pwy = ny_;
-    pwz = nz_;
-  }
-  if (!ok) {
-    // a pipeline wait ran out: flag it and drain the copies this block issued
-    if (tid == 0) {
-      atomicOr(a.err, 2);
-      for (int p = max(ibase, issued - NSLOT + 1); p <= issued; p++) {
-        const int q = p - ibase;
-        mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1);
-      }
-    }
-    __syncthreads();
-  }
+  tile_block<S, TJ>(a, base, r, s, tt, tid);
 }
 
 // ---------------------------------------------------------------------------

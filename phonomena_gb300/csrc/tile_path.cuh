@@ -1,0 +1,363 @@
+// Tile path of the fused step kernel (included by fdtd_step.cu).
+//
+// A block owns a (TJ x 32) tile of the (y, z) plane and marches along x over
+// planes [ib, ie).  Planes of u (3 components, 1-node halo) and material ids
+// arrive by TMA in a 4-slot ring.  Every smem access uses offsets fixed per
+// thread (own position Lu / Lm, neighbours at constant distance), the range
+// predicates of the reference's slices are split into per-thread (j, k) and
+// per-plane (i) parts computed once, and the per-axis spacings live in
+// registers, so the inner loop is the stencil arithmetic plus shared-memory
+// traffic.  The arithmetic goes through the same scheme primitives (tn1, ts,
+// div3, div_surf_ref, update_value) as the face path, operation for
+// operation.
+// Included inside namespace phono, after SmemPlan and the scheme primitives.
+#pragma once
+
+template <class S, int TJ>
+__device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, unsigned char* base,
+                                           const Roles<typename S::R>& r, const typename S::R s, const int tt,
+                                           const int tid) {
+  using R = typename S::R;
+  using P = SmemPlan<R, TJ>;
+  using TF = TileFetch<R, TJ>;
+  constexpr int NT = TK * TJ;
+  constexpr int W = P::W, PL = P::PL;
+  constexpr int KW = TF::KW, KB = TF::KB, CW = TF::CW, SU = TF::SU, SM = TF::SM;
+  constexpr int XO = 0, YO = CW, ZO = 2 * CW;  // component offsets inside a ring slot
+
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base);
+  R* stab = reinterpret_cast<R*>(base + P::off_tab);
+  R* uring = reinterpret_cast<R*>(base + P::off_u);
+  uint8_t* mring = reinterpret_cast<uint8_t*>(base + P::off_m);
+  R* sT2 = reinterpret_cast<R*>(base + P::off_t);
+  R* sT3 = sT2 + PL;
+  R* sT4 = sT3 + PL;
+  R* sT5 = sT4 + PL;      // [2][PL]
+  R* sT6 = sT5 + 2 * PL;  // [2][PL]
+
+  const Geo& g = a.g;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int b = blockIdx.x;
+  const int kt = b % a.ntk;
+  const int rest = b / a.ntk;
+  const int jt = rest % a.ntj;
+  const int seg = rest / a.ntj;
+  const int j0 = jt * TJ, k0 = kt * TK;
+  const int ib = seg * a.xseg;
+  const int ie = min(ib + a.xseg, nx - 1);
+  const int ibase = ib - 1;
+  const int plast = ie + 1;  // last plane the segment reads
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j = j0 + ty, k = k0 + tx;
+  const bool active = (j < ny - 1) && (k < nz - 1);
+  const int L = (ty + 1) * W + tx + 1;    // own entry of the stress planes
+  const int Lu = (ty + 1) * KW + tx + KB;  // own entry of a u component tile
+  const int Lm = (ty + 1) * MKW + tx + MKOFF;
+
+  const bool tab_in_smem = a.nmat <= TAB_SMEM;
+  if (tab_in_smem)
+    for (int q = tid; q < a.nmat * 16; q += NT) stab[q] = __ldg(a.tab + q);
+  const R* tab = tab_in_smem ? stab : a.tab;
+
+  // -------- per-thread constants (own position) --------
+  // stress ranges of the reference (base_solver.py:329-372, 408-433)
+  const bool k_in = k <= nz - 2;               // all six stresses need k <= nz-2
+  const bool j_n = j >= 1 && j <= ny - 2;      // T1..T3, T5: j in [1, ny-2]
+  const bool j_s = j <= ny - 2;                // T4, T6: j in [0, ny-2]
+  const bool kz = k == 0;                      // traction-free row
+  const R sdy_m = j >= 1 && j <= ny - 2 ? __ldg(a.sp.sdy + j - 1) : R(1);
+  const R fdy_j = j <= ny - 2 ? __ldg(a.sp.fdy + j) : R(1);
+  const R sdz_m = k >= 1 && k <= nz - 2 ? __ldg(a.sp.sdz + k - 1) : R(1);
+  const R fdz_k = k <= nz - 2 ? __ldg(a.sp.fdz + k) : R(1);
+  // spacings as used by the z = 0 row or the interior
+  const R t123_b = kz ? a.sp.sdy0 : sdy_m, t123_d = kz ? a.sp.sdz0 : sdz_m;
+  // output classification (component extents, faces, V0 sets)
+  const bool face_y = j == 0 || j == ny - 2;  // uy: y = 0 / y = N faces
+  const bool face_z = j == 0 || k == nz - 2;  // uz: y = 0 / z = N faces
+  const bool face_x = j == 0;                 // ux: y = 0 face (x = N checked per plane)
+
+  // -------- TMA ring --------
+  auto issue = [&](int p) {  // plane p into its ring slot (one thread)
+    const int q = p - ibase, sl = q & (NSLOT - 1);
+    mbar_expect_tx(&bars[sl], P::tx_bytes);
+    // padded coordinates: k + KOFF, j + 1, i + 1; the tiles start at k0-KB, j0-1
+    tma_load_4d(uring + sl * SU, &a.tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
+    tma_load_3d(mring + sl * SM, &a.tm_mat, k0, j0, p + 1, &bars[sl]);
+  };
+  bool ok = true;
+  auto wait_plane = [&](int p) {
+    const int q = p - ibase;
+    if (!mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1)) ok = false;
+  };
+  auto uslot = [&](int p) { return uring + ((p - ibase) & (NSLOT - 1)) * SU; };
+  auto mslot = [&](int p) { return mring + ((p - ibase) & (NSLOT - 1)) * SM; };
+
+  if (tid == 0) {
+    for (int q = 0; q < NSLOT; q++) mbar_init(&bars[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int issued = ibase - 1;  // last plane issued (thread 0)
+  if (tid == 0)
+    for (int p = ibase; p <= min(ibase + NSLOT - 1, plast); p++) {
+      issue(p);
+      issued = p;
+    }
+
+  // prologue: planes ib-1 and ib; source patch (plane 0 is in the ring when
+  // it is plane ib or ib-1)
+  wait_plane(ib - 1);
+  wait_plane(ib);
+  if (ib <= 1) {
+    R* zt = uslot(0) + ZO;
+    if (a.source_mode == 1) {
+      for (int q = tid; q < CW; q += NT) zt[q] = s;
+    } else if (k0 == 0) {
+      for (int q = tid; q < TJ + 2; q += NT) zt[q * KW + KB] = s;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+
+  // -------- stress evaluators on plane pointers --------
+  // U0/Up: u tiles of planes i and i+1 (Um: i-1); M0/Mp material tiles of i, i+1.
+  // d = offset of the evaluated position from the own one inside a tile.
+  // T1..T3 at (i, j+dj, k+dk): the caller supplies validity and spacings.
+  auto T123 = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, bool kzero, R sa, R sb, R sd,
+                  R& T1, R& T2, R& T3, bool want3) {
+    const R* c = tab + 16 * M0[Lm + dm];
+    const R d1 = S::sub(U0[XO + Lu + du], Um[XO + Lu + du]);
+    const R d2 = S::sub(U0[YO + Lu + du], U0[YO + Lu + du - KW]);
+    const R d3 = kzero ? U0[ZO + Lu + du] : S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
+    T1 = S::tn1(c, d1, d2, d3, sa, sb, sd);
+    T2 = S::tn1(c + 3, d1, d2, d3, sa, sb, sd);
+    T3 = want3 ? S::tn1(c + 6, d1, d2, d3, sa, sb, sd) : R(0);
+  };
+  // T4 (base_solver.py:353-358, 420-423)
+  auto T4f = [&](const R* U0, const uint8_t* M0, int du, int dm, bool kzero, R fz, R fy) {
+    const R c = tab[16 * M0[Lm + dm + MKW + (kzero ? 0 : 1)] + 9];
+    const R d1 = S::sub(U0[YO + Lu + du + 1], U0[YO + Lu + du]);
+    const R d2 = S::sub(U0[ZO + Lu + du + KW], U0[ZO + Lu + du]);
+    return kzero ? S::ts(c, d1, a.sp.fdy0, d2, a.sp.fdz0) : S::ts(c, d1, fz, d2, fy);
+  };
+  // T5 (base_solver.py:360-365, 425-428)
+  auto T5f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fz, R fx) {
+    const R c = tab[16 * Mp[Lm + dm + (kzero ? 0 : 1)] + 10];
+    const R d1 = S::sub(U0[XO + Lu + du + 1], U0[XO + Lu + du]);
+    const R d2 = S::sub(Up[ZO + Lu + du], U0[ZO + Lu + du]);
+    return kzero ? S::ts(c, d1, a.sp.fdx0, d2, a.sp.fdz0) : S::ts(c, d1, fz, d2, fx);
+  };
+  // T6 (base_solver.py:367-372, 430-433)
+  auto T6f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fy, R fx) {
+    const R c = tab[16 * Mp[Lm + dm + MKW] + 11];
+    const R d1 = S::sub(U0[XO + Lu + du + KW], U0[XO + Lu + du]);
+    const R d2 = S::sub(Up[YO + Lu + du], U0[YO + Lu + du]);
+    return kzero ? S::ts(c, d1, a.sp.fdx0, d2, a.sp.fdz0) : S::ts(c, d1, fy, d2, fx);
+  };
+
+  // prologue stresses: own T5, T6 at plane ib-1
+  R t5m, t6m;
+  {
+    const int i = ib - 1;
+    const bool i_s = i >= 0 && i <= nx - 2;
+    const R fx = i_s ? __ldg(a.sp.fdx + i) : R(1);
+    const R* U0 = uslot(i);
+    const R* Up = uslot(i + 1);
+    const uint8_t* Mp = mslot(i + 1);
+    t5m = (i_s && j_n && k_in) ? T5f(U0, Up, Mp, 0, 0, kz, fdz_k, fx) : R(0);
+    t6m = (i_s && j_s && k_in) ? T6f(U0, Up, Mp, 0, 0, kz, fdy_j, fx) : R(0);
+  }
+  R t1m = 0, uxm = 0;
+
+  // pointwise state prefetch, one plane ahead: ux at plane i-1, uy/uz at plane i
+  // (V0 points only: u_new there depends on u_old / v / c of the same point)
+  const long long off_j = g.o0 + (long long)j * g.sy + k;
+  auto want_y = [&](int i) { return active && i < ie && !face_y && i >= 1 && i <= nx - 2; };
+  auto want_z = [&](int i) { return active && i < ie && !face_z && i >= 1 && i <= nx - 2 && j_n; };
+  auto want_x = [&](int i) { return active && i > ib && i - 1 < ie && !face_x && i - 1 != nx - 2 && j_n; };
+  Pw<R> pwx{0, 0}, pwy{0, 0}, pwz{0, 0};
+  if (want_y(ib)) pwy = load_pw<S>(r, 1, off_j + (long long)ib * g.sx);
+  if (want_z(ib)) pwz = load_pw<S>(r, 2, off_j + (long long)ib * g.sx);
+
+  for (int i = ib; i <= ie; i++) {
+    const long long off_i = off_j + (long long)i * g.sx;  // (i, j, k)
+    Pw<R> nx_{0, 0}, ny_{0, 0}, nz_{0, 0};
+    if (want_x(i + 1)) nx_ = load_pw<S>(r, 0, off_i);
+    if (want_y(i + 1)) ny_ = load_pw<S>(r, 1, off_i + g.sx);
+    if (want_z(i + 1)) nz_ = load_pw<S>(r, 2, off_i + g.sx);
+    // per-plane (uniform) predicates and spacings
+    const bool i_n = i >= 1 && i <= nx - 2;  // T1..T4
+    const bool i_s = i <= nx - 2;            // T5, T6 (i >= 0 here)
+    const R fdx_i = i_s ? __ldg(a.sp.fdx + i) : R(1);
+    const R sdx_im = i_n ? __ldg(a.sp.sdx + i - 1) : R(1);
+    const R fdx_im = i >= 1 ? __ldg(a.sp.fdx + i - 1) : R(1);
+    wait_plane(i + 1);
+    if (__syncthreads_or(!ok)) break;
+    const int p = i & 1;
+    const R* Um = uslot(i - 1);
+    const R* U0 = uslot(i);
+    const R* Up = uslot(i + 1);
+    const uint8_t* M0 = mslot(i);
+    const uint8_t* Mp = mslot(i + 1);
+    // own stresses at plane i
+    R t1c, t2c, t3c;
+    if (i_n && j_n && k_in) {
+      T123(Um, U0, M0, 0, 0, kz, kz ? a.sp.sdx0 : sdx_im, t123_b, t123_d, t1c, t2c, t3c, !kz);
+    } else {
+      t1c = t2c = t3c = R(0);
+    }
+    const R t4c = (i_n && j_s && k_in) ? T4f(U0, M0, 0, 0, kz, fdz_k, fdy_j) : R(0);
+    const R t5c = (i_s && j_n && k_in) ? T5f(U0, Up, Mp, 0, 0, kz, fdz_k, fdx_i) : R(0);
+    const R t6c = (i_s && j_s && k_in) ? T6f(U0, Up, Mp, 0, 0, kz, fdy_j, fdx_i) : R(0);
+    sT2[L] = t2c;
+    sT3[L] = t3c;
+    sT4[L] = t4c;
+    sT5[p * PL + L] = t5c;
+    sT6[p * PL + L] = t6c;
+    // halo stresses the neighbours need: T2 row j0+TJ, T6/T4 row j0-1,
+    // T3 column k0+TK, T4/T5 column k0-1.  Offsets are relative to the thread
+    // at (ty, tx) = (0, 0) of the tile, so Lu/Lm must be subtracted back.
+    for (int qq = tid; qq < 3 * TK + 3 * TJ; qq += NT) {
+      const int du0 = -Lu + KW + KB, dm0 = -Lm + MKW + MKOFF;  // shift to tile origin (jl=0, kl=0)
+      if (qq < TK) {  // T2 at (j0+TJ, k0+qq)
+        const int jj = j0 + TJ, kk = k0 + qq;
+        R v = R(0);
+        if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2) {
+          const bool z0 = kk == 0;
+          R x1, x2, x3;
+          T123(Um, U0, M0, du0 + TJ * KW + qq, dm0 + TJ * MKW + qq, z0, z0 ? a.sp.sdx0 : sdx_im,
+               z0 ? a.sp.sdy0 : __ldg(a.sp.sdy + jj - 1), z0 ? a.sp.sdz0 : __ldg(a.sp.sdz + kk - 1), x1, x2, x3,
+               false);
+          v = x2;
+        }
+        sT2[(TJ + 1) * W + qq + 1] = v;
+      } else if (qq < 2 * TK) {  // T6 at (j0-1, k0+q)
+        const int q = qq - TK, jj = j0 - 1, kk = k0 + q;
+        R v = R(0);
+        if (i_s && jj >= 0 && jj <= ny - 2 && kk <= nz - 2)
+          v = T6f(U0, Up, Mp, du0 - KW + q, dm0 - MKW + q, kk == 0, __ldg(a.sp.fdy + jj), fdx_i);
+        sT6[p * PL + q + 1] = v;
+      } else if (qq < 3 * TK) {  // T4 at (j0-1, k0+q)
+        const int q = qq - 2 * TK, jj = j0 - 1, kk = k0 + q;
+        R v = R(0);
+        if (i_n && jj >= 0 && jj <= ny - 2 && kk <= nz - 2)
+          v = T4f(U0, M0, du0 - KW + q, dm0 - MKW + q, kk == 0, __ldg(a.sp.fdz + kk), __ldg(a.sp.fdy + jj));
+        sT4[q + 1] = v;
+      } else {
+        const int w = qq - 3 * TK;
+        const int which = w / TJ, jl = w - which * TJ;
+        const int jj = j0 + jl;
+        if (which == 0) {  // T3 at (j0+jl, k0+TK)
+          const int kk = k0 + TK;
+          R v = R(0);
+          if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2) {
+            R x1, x2, x3;  // kk >= 32: never the z = 0 row
+            T123(Um, U0, M0, du0 + jl * KW + TK, dm0 + jl * MKW + TK, false, sdx_im, __ldg(a.sp.sdy + jj - 1),
+                 __ldg(a.sp.sdz + kk - 1), x1, x2, x3, true);
+            v = x3;
+          }
+          sT3[(jl + 1) * W + TK + 1] = v;
+        } else if (which == 1) {  // T4 at (j0+jl, k0-1)
+          const int kk = k0 - 1;
+          R v = R(0);
+          if (i_n && jj <= ny - 2 && kk >= 0 && kk <= nz - 2)
+            v = T4f(U0, M0, du0 + jl * KW - 1, dm0 + jl * MKW - 1, kk == 0, __ldg(a.sp.fdz + kk),
+                    __ldg(a.sp.fdy + jj));
+          sT4[(jl + 1) * W] = v;
+        } else {  // T5 at (j0+jl, k0-1)
+          const int kk = k0 - 1;
+          R v = R(0);
+          if (i_s && jj >= 1 && jj <= ny - 2 && kk >= 0 && kk <= nz - 2)
+            v = T5f(U0, Up, Mp, du0 + jl * KW - 1, dm0 + jl * MKW - 1, kk == 0, __ldg(a.sp.fdz + kk), fdx_i);
+          sT5[p * PL + (jl + 1) * W] = v;
+        }
+      }
+    }
+    const R uxc = U0[XO + Lu], uyc = U0[YO + Lu], uzc = U0[ZO + Lu];
+    __syncthreads();
+    // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
+    if (tid == 0 && i - 1 + NSLOT <= plast) {
+      issue(i - 1 + NSLOT);
+      issued = i - 1 + NSLOT;
+    }
+    if (active) {
+      if (i < ie) {
+        // uy_new(i, j, k)   (base_solver.py:449-455, 503-509)
+        if (!face_y) {
+          if (i_n) {
+            const R* row = tab + 16 * M0[Lm + MKW];
+            const R dv = kz ? S::div3(S::sub(t6c, t6m), a.sp.sdx0, S::sub(sT2[L + W], t2c), a.sp.fdy0, t4c, a.sp.sdz0)
+                            : S::div3(S::sub(t6c, t6m), sdx_im, S::sub(sT2[L + W], t2c), fdy_j,
+                                      S::sub(t4c, sT4[L - 1]), sdz_m);
+            R vn, cn;
+            const R un = update_value<S>(uyc, pwy, dv, row, vn, cn);
+            store_point<S>(r, 1, off_i, un, vn, cn);
+          } else {
+            store_stale<S>(r, 1, off_i);
+          }
+        }
+        // uz_new(i, j, k)   (base_solver.py:457-463, 511-516)
+        if (!face_z) {
+          R val;
+          if (i_n && j_n) {
+            R dv;
+            const R* row;
+            if (kz) {
+              row = tab + 16 * M0[Lm];  // density at z index 0 (base_solver.py:513)
+              dv = a.surface_mode == 0
+                       ? S::div_surf_ref(S::sub(t5c, t5m), a.sp.sdx0, S::sub(t4c, sT4[L - W]), a.sp.sdy0, sT3[L + 1])
+                       : S::div3(S::sub(t5c, t5m), a.sp.sdx0, S::sub(t4c, sT4[L - W]), a.sp.sdy0, sT3[L + 1],
+                                 a.sp.fdz0);
+            } else {
+              row = tab + 16 * M0[Lm + 1];
+              dv = S::div3(S::sub(t5c, t5m), sdx_im, S::sub(t4c, sT4[L - W]), sdy_m, S::sub(sT3[L + 1], t3c), fdz_k);
+            }
+            R vn, cn;
+            val = update_value<S>(uzc, pwz, dv, row, vn, cn);
+            store_point<S>(r, 2, off_i, val, vn, cn);
+          } else {
+            store_stale<S>(r, 2, off_i);
+            val = __ldg(r.cur(2) + off_i);
+          }
+          if (kz) record(a, tt, i, j, val);
+        }
+      }
+      if (i > ib && !face_x && i - 1 != nx - 2) {
+        // ux_new(i-1, j, k)   (base_solver.py:441-447, 495-501)
+        const long long off = off_i - g.sx;
+        if (j_n) {
+          const int pm = p ^ 1;
+          const R* row = tab + 16 * M0[Lm];  // P[(i-1)+1, j, k]
+          const R dv = kz ? S::div3(S::sub(t1c, t1m), a.sp.fdx0, S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]),
+                                    a.sp.sdy0, sT5[pm * PL + L], a.sp.sdz0)
+                          : S::div3(S::sub(t1c, t1m), fdx_im, S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]), sdy_m,
+                                    S::sub(sT5[pm * PL + L], sT5[pm * PL + L - 1]), sdz_m);
+          R vn, cn;
+          const R un = update_value<S>(uxm, pwx, dv, row, vn, cn);
+          store_point<S>(r, 0, off, un, vn, cn);
+        } else {
+          store_stale<S>(r, 0, off);
+        }
+      }
+    }
+    t1m = t1c;
+    t5m = t5c;
+    t6m = t6c;
+    uxm = uxc;
+    pwx = nx_;
+    pwy = ny_;
+    pwz = nz_;
+  }
+  if (!ok) {
+    // a pipeline wait ran out: flag it and drain the copies this block issued
+    if (tid == 0) {
+      atomicOr(a.err, 2);
+      for (int p = max(ibase, issued - NSLOT + 1); p <= issued; p++) {
+        const int q = p - ibase;
+        mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1);
+      }
+    }
+    __syncthreads();
+  }
+}
+
