@@ -30,7 +30,7 @@ constexpr int TK = 32;      // tile width along z (the contiguous axis): one war
 constexpr int NSLOT = 4;    // planes in the shared-memory ring
 constexpr int MKOFF = 8;    // material front pad in k (bytes)
 constexpr int MKW = 48;     // material tile width in k (bytes): k0-8 .. k0+40
-constexpr int TAB_SMEM = 32;  // material rows staged in shared memory
+constexpr int TAB_SMEM = 256;  // material rows staged in shared memory (all ids)
 
 template <class R>
 struct Lay;

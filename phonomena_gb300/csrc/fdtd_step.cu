@@ -505,9 +505,10 @@ struct SmemPlan {
 // ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
-// FP32: 32 resident warps per SM (64 registers, no spills); FP64: unconstrained
+// FP32: 32 resident warps per SM (64 registers, no spills); FP64: 16 warps
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : 1)) fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
+__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : (TJ < 16 ? 16 / TJ : 1)))
+    fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
   using P = SmemPlan<R, TJ>;
   using TF = TileFetch<R, TJ>;
