@@ -216,11 +216,9 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
     // halo stresses the neighbours need: T2 row j0+TJ, T6/T4 row j0-1,
     // T3 column k0+TK, T4/T5 column k0-1.  Offsets are relative to the thread
     // at (ty, tx) = (0, 0) of the tile, so Lu/Lm must be subtracted back.
-    // The NH tasks are dealt to the warps in contiguous runs of HPW, so every
-    // warp does about the same halo work and at most two stress kinds.
-    constexpr int NH = 3 * TK + 3 * TJ, NWARP = NT / 32, HPW = (NH + NWARP - 1) / NWARP;
-    static_assert(HPW <= 32, "halo tasks per warp exceed the warp width");
-    for (int qq = (tid >> 5) * HPW + (tid & 31); (tid & 31) < HPW && qq < NH; qq = NH) {
+    // Task qq runs on thread qq: each of the first three warps computes one
+    // row kind, the fourth the three column kinds.
+    for (int qq = tid; qq < 3 * TK + 3 * TJ; qq += NT) {
       const int du0 = -Lu + KW + KB, dm0 = -Lm + MKW + MKOFF;  // shift to tile origin (jl=0, kl=0)
       if (qq < TK) {  // T2 at (j0+TJ, k0+qq)
         const int jj = j0 + TJ, kk = k0 + qq;
