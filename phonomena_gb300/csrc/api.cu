@@ -65,7 +65,7 @@ struct phono_handle {
   double2* partial = nullptr;
   double* energy_out = nullptr;
   double abc[8] = {};
-  int tj = 8, xseg = 64, ntj = 0, ntk = 0, nseg = 0, n_tile = 0, n_face = 0;
+  int tj = 8, xseg = 64, ntj = 0, ntk = 0, nseg = 0, n_tile = 0, n_face = 0, separate_faces = 1;
   FaceTable faces{};
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -219,8 +219,9 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
 }
 
 static cudaError_t launch_one(phono_handle* h, int step_off) {
-  if (h->d.precision == PHONO_F64) return launch_step_f64(make_args<double>(h, step_off), h->tj, h->n_face, h->stream);
-  return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->n_face, h->stream);
+  if (h->d.precision == PHONO_F64)
+    return launch_step_f64(make_args<double>(h, step_off), h->tj, h->separate_faces, h->stream);
+  return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->separate_faces, h->stream);
 }
 
 static int check_desc(const phono_desc* d) {
@@ -386,6 +387,9 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->faces.off[12] = (int)acc;
   int nt = TK * h->tj;
   long long nface = (acc + nt - 1) / nt;
+  // faces in a second launch that reads the tile pass's interior values; the
+  // chain end of a face point can itself be a face point only when ny == 3
+  h->separate_faces = ny >= 4 ? 1 : 0;
   if (ntile + nface > 0x7fffffffLL || acc > 0x7fffffffLL) {
     delete h;
     return fail(PHONO_ERR_ARG, "grid too large for one launch");

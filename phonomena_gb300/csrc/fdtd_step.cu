@@ -413,9 +413,14 @@ __device__ typename S::R v0_global(const StepArgs<typename S::R>& a, const Roles
 
 // final value of a face point: walk z=N, y=N, y=0, x=N (reverse of the
 // reference order), evaluate the interior value at the end, apply the faces
+// from_out: the interior value of the chain end is read from the new state,
+// which the tile pass has already written (separate face pass); otherwise it
+// is evaluated here from the input state (fused launch).  The chain end is
+// never a face point when ny >= 4, which is when the separate pass is used.
 template <class S>
 __device__ typename S::R face_value(const StepArgs<typename S::R>& a, const Roles<typename S::R>& r,
-                                    const GlobalFetch<typename S::R>& f, int c, int i, int j, int k) {
+                                    const GlobalFetch<typename S::R>& f, int c, int i, int j, int k,
+                                    bool from_out) {
   using R = typename S::R;
   const Geo& g = a.g;
   const int xi = ext_x(g, c) - 1, jN = ext_y(g, c) - 1, kz = ext_z(g, c) - 1;
@@ -432,12 +437,45 @@ __device__ typename S::R face_value(const StepArgs<typename S::R>& a, const Role
   auto U = [&](int ii, int jj, int kk) -> R {
     return c == 0 ? f.x(ii, jj, kk) : (c == 1 ? f.y(ii, jj, kk) : f.z(ii, jj, kk));
   };
-  R val = v0_global<S>(a, r, f, c, ci, cj, ck);
+  R val = from_out ? r.out(c)[fidx(g, ci, cj, ck)] : v0_global<S>(a, r, f, c, ci, cj, ck);
   if (sx) val = S::abc(c == 0 ? a.abc[0] : a.abc[1], val, U(xi, cj, ck), U(xi - 1, cj, ck));
   if (sy0) val = S::abc(c == 1 ? a.abc[3] : a.abc[2], val, U(i, 0, kyn), U(i, 1, kyn));
   if (syn) val = S::abc(c == 1 ? a.abc[5] : a.abc[4], val, U(i, jN, kyn), U(i, jN - 1, kyn));
   if (sz) val = S::abc(c == 2 ? a.abc[7] : a.abc[6], val, U(i, j, kz), U(i, j, kz - 1));
   return val;
+}
+
+// one face point: flattened index -> (component, plane, i, j, k), final value,
+// state store and surface record
+template <class S>
+__device__ __forceinline__ void face_point(const StepArgs<typename S::R>& a, const Roles<typename S::R>& r,
+                                           const typename S::R s, const int tt, const int idx, const bool from_out) {
+  using R = typename S::R;
+  const Geo& g = a.g;
+  if (idx >= a.faces.off[12]) return;
+  int q = 0;
+  while (q < 11 && idx >= a.faces.off[q + 1]) q++;
+  const int c = q >> 2, pl = q & 3, rr = idx - a.faces.off[q];
+  const int ex = ext_x(g, c), ey = ext_y(g, c), ez = ext_z(g, c);
+  int i, j, k;
+  if (pl == 0) { i = rr / ey; j = rr - i * ey; k = ez - 1; }
+  else if (pl == 1) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = ey - 1; }
+  else if (pl == 2) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = 0; }
+  else { j = rr / (ez - 1); k = rr - j * (ez - 1); j += 1; i = ex - 1; }
+  GlobalFetch<R> f{r.cur(0), r.cur(1), r.cur(2), a.mat, a.tab, g, s, a.source_mode};
+  R val = a.bc == 1 ? R(0) : face_value<S>(a, r, f, c, i, j, k, from_out);
+  long long off = fidx(g, i, j, k);
+  store_point<S>(r, c, off, val, R(0), R(0));
+  if (c == 2 && k == 0) record(a, tt, i, j, val);
+}
+
+// separate face pass: runs after the tile-only step launch on the same stream
+template <class S>
+__global__ void __launch_bounds__(256) fdtd_face_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
+  using R = typename S::R;
+  const int tt = __ldg(a.step_base) + a.step_off;
+  const Roles<R> r = roles<S>(a, tt);
+  face_point<S>(a, r, (R)__ldg(a.src + tt), tt, blockIdx.x * 256 + threadIdx.x, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -514,8 +552,11 @@ __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ 
   using TF = TileFetch<R, TJ>;
   constexpr int NT = TK * TJ;
   constexpr int W = P::W, PL = P::PL;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // 128-byte aligned start, derived by pointer arithmetic on the shared array
+  // so that every access below stays a shared-memory access (an integer
+  // round trip would turn them into generic loads)
+  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
   const Geo& g = a.g;
   const int tt = __ldg(a.step_base) + a.step_off;
@@ -524,23 +565,8 @@ __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ 
   const int tid = threadIdx.y * TK + threadIdx.x;
 
   if ((int)blockIdx.x >= a.n_tile_blocks) {
-    // ---------------- face blocks ----------------
-    int idx = ((int)blockIdx.x - a.n_tile_blocks) * NT + tid;
-    if (idx >= a.faces.off[12]) return;
-    int q = 0;
-    while (q < 11 && idx >= a.faces.off[q + 1]) q++;
-    const int c = q >> 2, pl = q & 3, rr = idx - a.faces.off[q];
-    const int ex = ext_x(g, c), ey = ext_y(g, c), ez = ext_z(g, c);
-    int i, j, k;
-    if (pl == 0) { i = rr / ey; j = rr - i * ey; k = ez - 1; }
-    else if (pl == 1) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = ey - 1; }
-    else if (pl == 2) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = 0; }
-    else { j = rr / (ez - 1); k = rr - j * (ez - 1); j += 1; i = ex - 1; }
-    GlobalFetch<R> f{r.cur(0), r.cur(1), r.cur(2), a.mat, a.tab, g, s, a.source_mode};
-    R val = a.bc == 1 ? R(0) : face_value<S>(a, r, f, c, i, j, k);
-    long long off = fidx(g, i, j, k);
-    store_point<S>(r, c, off, val, R(0), R(0));
-    if (c == 2 && k == 0) record(a, tt, i, j, val);
+    // ---------------- face blocks (fused launch) ----------------
+    face_point<S>(a, r, s, tt, ((int)blockIdx.x - a.n_tile_blocks) * NT + tid, false);
     return;
   }
 
@@ -578,19 +604,22 @@ cudaError_t configure_step(int tj) {
 }
 
 template <class S, int TJ>
-static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int n_face_blocks, cudaStream_t st) {
+static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_faces, cudaStream_t st) {
+  const int nfaces = a.faces.off[12];
   dim3 block(TK, TJ);
-  dim3 grid(a.n_tile_blocks + n_face_blocks);
+  // fused: face points handled by extra blocks of the same launch
+  dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + TK * TJ - 1) / (TK * TJ)));
   fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<typename S::R, TJ>::total, st>>>(a);
+  if (separate_faces && nfaces > 0) fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 
 template <class S>
-cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int n_face_blocks, cudaStream_t st) {
+cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int separate_faces, cudaStream_t st) {
   switch (tj) {
-    case 4: return launch_tj<S, 4>(a, n_face_blocks, st);
-    case 8: return launch_tj<S, 8>(a, n_face_blocks, st);
-    case 16: return launch_tj<S, 16>(a, n_face_blocks, st);
+    case 4: return launch_tj<S, 4>(a, separate_faces, st);
+    case 8: return launch_tj<S, 8>(a, separate_faces, st);
+    case 16: return launch_tj<S, 16>(a, separate_faces, st);
     default: return cudaErrorInvalidValue;
   }
 }
