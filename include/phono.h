@@ -149,6 +149,43 @@ int phono_elem_size(const phono_handle *h);
  * counterpart (error metric). */
 int phono_energy(phono_handle *h, double out[2]);
 
+/* Energy of a state held in the caller's own device buffers, computed
+ * without allocating anything.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc/cudaFree: code that runs while a
+ * stream is being captured into a CUDA graph, applications whose device
+ * memory is owned by another allocator (a framework's caching pool, a fixed
+ * reservation), and latency-bound loops that must not take the implicit
+ * device synchronisation of cudaFree.  The per-plane partial sums go to a
+ * file-scope __device__ scratch array of PHONO_ENERGY_STATIC_MAX_NX entries
+ * (128 KiB, held by every GPU that loads the library until exit); nx above
+ * that limit is rejected with PHONO_ERR_ARG.  All calls share that array:
+ * calls whose kernels overlap on the GPU race on it and must be serialised
+ * by the caller (one stream, or events).  Every call overwrites the partials
+ * it reads, so nothing has to be cleared between calls.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ *
+ * Inputs are dense arrays in the reference shapes, element type given by
+ * `precision`, all device pointers; out_dev receives two doubles
+ * (kinetic, strain) in device memory, written on `stream` (a cudaStream_t,
+ * NULL for the default stream); the call does not synchronise. */
+#define PHONO_ENERGY_STATIC_MAX_NX 8192
+
+typedef struct phono_energy_dense {
+  int nx, ny, nz;                /* mesh nodes, 3 <= nx <= PHONO_ENERGY_STATIC_MAX_NX */
+  int precision;                 /* PHONO_F64: velocity from (u - u_old)/dt; PHONO_F32K: v given */
+  const void *ux, *uy, *uz;      /* displacement (double for F64, float for F32K) */
+  const void *vx, *vy, *vz;      /* F32K: velocity; F64: u at the previous step */
+  const uint8_t *mat;            /* nx*ny*nz node material ids */
+  const double *table;           /* material rows of PHONO_TABLE_COLS doubles */
+  const double *fdx, *fdy, *fdz; /* full spacings (n-1 values) */
+  const double *sdx, *sdy, *sdz; /* staggered spacings (n-2 values) */
+  double dt;
+} phono_energy_dense;
+
+int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *stream);
+
 /* Device time of the last phono_step call in milliseconds (CUDA events). */
 int phono_last_step_ms(phono_handle *h, float *ms);
 

@@ -25,6 +25,7 @@ FIELDS = {"ux": 0, "uy": 1, "uz": 2, "ux_old": 3, "uy_old": 4, "uz_old": 5,
 EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done", "phono_reset",
            "phono_set_materials", "phono_stream", "phono_sync",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
+           "phono_energy_static",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
 
@@ -46,6 +47,21 @@ class PhonoDesc(ctypes.Structure):
         ("tile_j", ctypes.c_int), ("x_segment", ctypes.c_int),
     ]
 
+
+class PhonoEnergyDense(ctypes.Structure):
+    """phono_energy_dense of include/phono.h: caller-owned dense device arrays."""
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("precision", ctypes.c_int),
+        ("ux", ctypes.c_void_p), ("uy", ctypes.c_void_p), ("uz", ctypes.c_void_p),
+        ("vx", ctypes.c_void_p), ("vy", ctypes.c_void_p), ("vz", ctypes.c_void_p),
+        ("mat", ctypes.c_void_p), ("table", ctypes.c_void_p),
+        ("fdx", ctypes.c_void_p), ("fdy", ctypes.c_void_p), ("fdz", ctypes.c_void_p),
+        ("sdx", ctypes.c_void_p), ("sdy", ctypes.c_void_p), ("sdz", ctypes.c_void_p),
+        ("dt", ctypes.c_double),
+    ]
+
+
+ENERGY_STATIC_MAX_NX = 8192
 
 _lib = None
 
@@ -74,6 +90,7 @@ def load(path: Path | None = None):
         "phono_upload": (ci, [vp, ci, vp, ctypes.c_size_t]),
         "phono_elem_size": (ci, [vp]),
         "phono_energy": (ci, [vp, vp]),
+        "phono_energy_static": (ci, [ctypes.POINTER(PhonoEnergyDense), vp, vp]),
         "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_destroy": (None, [vp]),
         "phono_last_error": (ctypes.c_char_p, []),

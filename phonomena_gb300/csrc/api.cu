@@ -28,6 +28,10 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+namespace phono {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace phono
+
 #define CK(call)                                                                        \
   do {                                                                                  \
     cudaError_t e_ = (call);                                                            \

@@ -10,10 +10,11 @@
 // Pass 1 writes one partial pair per block into a scratch array; pass 2 sums
 // the partials in block order in one block, so the result does not depend on
 // scheduling.
+#include <cstdio>
+
 #include "fdtd_common.cuh"
 
 namespace phono {
-
 
 __device__ __forceinline__ double ld(const void* p, int f32, long long off) {
   return f32 ? (double)__ldg((const float*)p + off) : __ldg((const double*)p + off);
@@ -132,3 +133,133 @@ cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, do
 }
 
 }  // namespace phono
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (phono_energy_static in include/phono.h).
+//
+// Same energy as energy_partial_kernel, over caller-owned dense arrays in the
+// reference shapes, one block per x plane; the per-plane partials go to the
+// file-scope scratch array below instead of a buffer from cudaMalloc, and
+// energy_final_kernel sums them in plane order.  Host code must not pass the
+// array's name to a kernel (it is a host-side stand-in): the device address
+// is looked up once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+#include "../../include/phono.h"
+
+namespace phono {
+
+static __device__ __align__(256) double2 g_energy_scratch[PHONO_ENERGY_STATIC_MAX_NX];
+
+__global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_dense a, double2* __restrict__ partial) {
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int i = blockIdx.x;
+  const int f32 = a.precision == PHONO_F32K;
+  const double inv_dt = 1.0 / a.dt;
+  auto ix = [&](int ii, int jj, int kk) { return ((long long)ii * ny + jj) * nz + kk; };          // ux, mat
+  auto iy = [&](int ii, int jj, int kk) { return ((long long)ii * (ny - 1) + jj) * nz + kk; };    // uy
+  auto iz = [&](int ii, int jj, int kk) { return ((long long)ii * ny + jj) * (nz - 1) + kk; };    // uz
+  auto rho = [&](int ii, int jj, int kk) { return a.table[a.mat[ix(ii, jj, kk)] * 13 + 12]; };
+  auto C = [&](int ii, int jj, int kk, int e) { return a.table[a.mat[ix(ii, jj, kk)] * 13 + e]; };
+  auto vel = [&](const void* u, const void* v, long long off) {
+    double x = ld(v, f32, off);
+    return f32 ? x : (ld(u, 0, off) - x) * inv_dt;
+  };
+  double ek = 0.0, es = 0.0;
+  for (int q = threadIdx.x; q < ny * nz; q += EN_THREADS) {
+    const int j = q / nz, k = q - j * nz;
+    if (i <= nx - 3 && j >= 1 && j <= ny - 2 && k <= nz - 2) {
+      double v = vel(a.ux, a.vx, ix(i, j, k));
+      ek += 0.5 * rho(i + 1, j, k) * v * v;
+    }
+    if (i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 3 && k <= nz - 2) {
+      double v = vel(a.uy, a.vy, iy(i, j, k));
+      ek += 0.5 * rho(i, j + 1, k) * v * v;
+    }
+    if (i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2 && k <= nz - 3) {
+      double v = vel(a.uz, a.vz, iz(i, j, k));
+      ek += 0.5 * rho(i, j, k + 1) * v * v;
+    }
+    if (i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
+      double e1 = (ld(a.ux, f32, ix(i, j, k)) - ld(a.ux, f32, ix(i - 1, j, k))) / a.sdx[i - 1];
+      double e2 = (ld(a.uy, f32, iy(i, j, k)) - ld(a.uy, f32, iy(i, j - 1, k))) / a.sdy[j - 1];
+      double e3 = (ld(a.uz, f32, iz(i, j, k)) - ld(a.uz, f32, iz(i, j, k - 1))) / a.sdz[k - 1];
+      double t1 = C(i, j, k, 0) * e1 + C(i, j, k, 1) * e2 + C(i, j, k, 2) * e3;
+      double t2 = C(i, j, k, 3) * e1 + C(i, j, k, 4) * e2 + C(i, j, k, 5) * e3;
+      double t3 = C(i, j, k, 6) * e1 + C(i, j, k, 7) * e2 + C(i, j, k, 8) * e3;
+      es += 0.5 * (t1 * e1 + t2 * e2 + t3 * e3);
+    }
+    if (i >= 1 && i <= nx - 2 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
+      double gam = (ld(a.uy, f32, iy(i, j, k + 1)) - ld(a.uy, f32, iy(i, j, k))) / a.fdz[k] +
+                   (ld(a.uz, f32, iz(i, j + 1, k)) - ld(a.uz, f32, iz(i, j, k))) / a.fdy[j];
+      es += 0.5 * C(i, j + 1, k + 1, 9) * gam * gam;
+    }
+    if (i <= nx - 2 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
+      double gam = (ld(a.ux, f32, ix(i, j, k + 1)) - ld(a.ux, f32, ix(i, j, k))) / a.fdz[k] +
+                   (ld(a.uz, f32, iz(i + 1, j, k)) - ld(a.uz, f32, iz(i, j, k))) / a.fdx[i];
+      es += 0.5 * C(i + 1, j, k + 1, 10) * gam * gam;
+    }
+    if (i <= nx - 2 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
+      double gam = (ld(a.ux, f32, ix(i, j + 1, k)) - ld(a.ux, f32, ix(i, j, k))) / a.fdy[j] +
+                   (ld(a.uy, f32, iy(i + 1, j, k)) - ld(a.uy, f32, iy(i, j, k))) / a.fdx[i];
+      es += 0.5 * C(i + 1, j + 1, k, 11) * gam * gam;
+    }
+  }
+  __shared__ double sk[EN_THREADS], ss[EN_THREADS];
+  sk[threadIdx.x] = ek;
+  ss[threadIdx.x] = es;
+  __syncthreads();
+  for (int w = EN_THREADS / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sk[threadIdx.x] += sk[threadIdx.x + w];
+      ss[threadIdx.x] += ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[i] = make_double2(sk[0], ss[0]);
+}
+
+}  // namespace phono
+
+namespace phono {
+void set_last_error(const char* msg);  // api.cu: message behind phono_last_error()
+}
+
+namespace {
+// device address of g_energy_scratch, looked up once per device
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices] = {};
+}  // namespace
+
+extern "C" int phono_energy_static(const phono_energy_dense* in, double* out_dev, void* stream) {
+  using namespace phono;
+  auto fail = [](int code, const char* msg) {
+    set_last_error(msg);
+    return code;
+  };
+  if (!in || !out_dev) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (in->nx < 3 || in->ny < 3 || in->nz < 3) return fail(PHONO_ERR_ARG, "nx, ny, nz must be >= 3 mesh nodes");
+  if (in->nx > PHONO_ENERGY_STATIC_MAX_NX)
+    return fail(PHONO_ERR_ARG, "nx exceeds PHONO_ENERGY_STATIC_MAX_NX, the planes of the static scratch array");
+  if ((long long)in->ny * in->nz > 0x7fffffffLL) return fail(PHONO_ERR_ARG, "ny * nz too large");
+  if (in->precision != PHONO_F64 && in->precision != PHONO_F32K) return fail(PHONO_ERR_ARG, "unknown precision");
+  if (!in->ux || !in->uy || !in->uz || !in->vx || !in->vy || !in->vz || !in->mat || !in->table || !in->fdx ||
+      !in->fdy || !in->fdz || !in->sdx || !in->sdy || !in->sdz)
+    return fail(PHONO_ERR_ARG, "NULL device pointer in the input");
+  if (!(in->dt > 0.0)) return fail(PHONO_ERR_ARG, "dt must be > 0");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return fail(PHONO_ERR_CUDA, "cudaGetDevice failed");
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_energy_scratch);
+    if (e != cudaSuccess || !p) return fail(PHONO_ERR_CUDA, "cudaGetSymbolAddress of the energy scratch failed");
+    g_scratch_addr[dev] = p;
+  }
+  double2* partial = static_cast<double2*>(g_scratch_addr[dev]);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  energy_plane_kernel<<<in->nx, EN_THREADS, 0, st>>>(*in, partial);
+  energy_final_kernel<<<1, EN_THREADS, 0, st>>>(partial, in->nx, out_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, cudaGetErrorString(e));
+  return PHONO_OK;
+}
