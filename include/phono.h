@@ -41,6 +41,7 @@ extern "C" {
 /* arithmetic scheme */
 #define PHONO_F64 0  /* reference leapfrog, IEEE op order of the reference */
 #define PHONO_F32K 1 /* FP32 velocity form, Kahan-compensated displacement */
+#define PHONO_F64V 2 /* the F32K scheme in FP64: fast FP64 reference for error figures */
 
 /* z = 0 displacement row (base_solver.py:511-516) */
 #define PHONO_SURFACE_REFERENCE 0 /* precedence as written at :516 */
@@ -61,10 +62,10 @@ extern "C" {
 #define PHONO_FIELD_UX_OLD 3 /* F64: u at the previous step */
 #define PHONO_FIELD_UY_OLD 4
 #define PHONO_FIELD_UZ_OLD 5
-#define PHONO_FIELD_VX 6 /* F32K: velocity at the last half step */
+#define PHONO_FIELD_VX 6 /* F32K, F64V: velocity at the last half step */
 #define PHONO_FIELD_VY 7
 #define PHONO_FIELD_VZ 8
-#define PHONO_FIELD_CX 9 /* F32K: Kahan compensation */
+#define PHONO_FIELD_CX 9 /* F32K, F64V: Kahan compensation */
 #define PHONO_FIELD_CY 10
 #define PHONO_FIELD_CZ 11
 
@@ -81,7 +82,7 @@ typedef struct phono_desc {
   const double *table;           /* nmat rows of PHONO_TABLE_COLS */
   int nmat;                      /* 1..256 */
   double dt;                     /* time step (Material.dt, material.py:80-93) */
-  int precision;                 /* PHONO_F64 | PHONO_F32K */
+  int precision;                 /* PHONO_F64 | PHONO_F32K | PHONO_F64V */
   int surface_mode;              /* PHONO_SURFACE_* */
   int bc;                        /* PHONO_BC_* */
   int source_mode;               /* PHONO_SOURCE_* */
@@ -130,13 +131,13 @@ void *phono_stream(phono_handle *h);
 int phono_sync(phono_handle *h);
 
 /* Copy surface records [first, first+count) to host: count * nx * ny values
- * (double for PHONO_F64, float for PHONO_F32K), record r = uz[:, :, 0]
+ * (float for PHONO_F32K, double otherwise), record r = uz[:, :, 0]
  * after global step (r+1)*record_every - 1.  Stands in for the per-step
  * uz dataset of the reference writer (base_solver.py:114-116,153-155). */
 int phono_read_surface(phono_handle *h, int first, int count, void *host_out);
 
 /* Copy a field of the current state to / from host (reference shape, element
- * size 8 for PHONO_F64 and 4 for PHONO_F32K).  Download of UX..UZ is what
+ * size 4 for PHONO_F32K, 8 otherwise).  Download of UX..UZ is what
  * the reference leaves in g.ux, g.uy, g.uz after run. */
 int phono_download(phono_handle *h, int field, void *host, size_t bytes);
 int phono_upload(phono_handle *h, int field, const void *host, size_t bytes);
@@ -174,9 +175,9 @@ int phono_energy(phono_handle *h, double out[2]);
 
 typedef struct phono_energy_dense {
   int nx, ny, nz;                /* mesh nodes, 3 <= nx <= PHONO_ENERGY_STATIC_MAX_NX */
-  int precision;                 /* PHONO_F64: velocity from (u - u_old)/dt; PHONO_F32K: v given */
-  const void *ux, *uy, *uz;      /* displacement (double for F64, float for F32K) */
-  const void *vx, *vy, *vz;      /* F32K: velocity; F64: u at the previous step */
+  int precision;                 /* PHONO_F64: velocity from (u - u_old)/dt; F32K / F64V: v given */
+  const void *ux, *uy, *uz;      /* displacement (float for F32K, double otherwise) */
+  const void *vx, *vy, *vz;      /* F32K / F64V: velocity; F64: u at the previous step */
   const uint8_t *mat;            /* nx*ny*nz node material ids */
   const double *table;           /* material rows of PHONO_TABLE_COLS doubles */
   const double *fdx, *fdy, *fdz; /* full spacings (n-1 values) */

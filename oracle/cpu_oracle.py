@@ -25,7 +25,8 @@ LIB = BUILD / "libphono_oracle.so"
 def build(force: bool = False) -> Path:
     """Compile the C restatement (no FMA contraction, OpenMP when present)."""
     BUILD.mkdir(exist_ok=True)
-    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+    newest = max(SRC.stat().st_mtime, (HERE / "velocity_form.inc").stat().st_mtime)
+    if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
         return LIB
     base = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC", "-std=c11",
             "-o", str(LIB) + ".tmp", str(SRC), "-lm"]
@@ -67,9 +68,11 @@ def lib():
         _lib.ora_f64_run.restype = ctypes.c_int
         _lib.ora_f64_run.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_F64State), ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
-        _lib.ora_f32k_run.restype = ctypes.c_int
-        _lib.ora_f32k_run.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_F32State), ctypes.c_int,
-                                      ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        for name in ("ora_run_f32k", "ora_run_f64v"):
+            fn = getattr(_lib, name)
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_F32State), ctypes.c_int,
+                           ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
         _lib.ora_abc_coeffs.restype = None
         _lib.ora_abc_coeffs.argtypes = [ctypes.POINTER(_Problem), ctypes.c_void_p]
         _lib.ora_max_threads.restype = ctypes.c_int
@@ -131,11 +134,15 @@ class F64State:
 
 
 class F32KState:
+    """Velocity-form state (u, v, Kahan term); dtype float32 (F32K) or float64 (F64V)."""
+
+    dtype = np.float32
+
     def __init__(self, prob: OracleProblem):
         shp = prob.shapes()
-        self.u = [np.zeros(s, np.float32) for s in shp]
-        self.v = [np.zeros(s, np.float32) for s in shp]
-        self.c = [np.zeros(s, np.float32) for s in shp]
+        self.u = [np.zeros(s, self.dtype) for s in shp]
+        self.v = [np.zeros(s, self.dtype) for s in shp]
+        self.c = [np.zeros(s, self.dtype) for s in shp]
 
     def _c(self):
         arrs = self.u + self.v + self.c
@@ -157,15 +164,30 @@ def run_f64(prob: OracleProblem, state: F64State | None = None, t0=0, nsteps=Non
     return state, surf
 
 
-def run_f32k(prob: OracleProblem, state: F32KState | None = None, t0=0, nsteps=None, record_every=0,
-             nthreads=0):
-    state = state or F32KState(prob)
+class F64VState(F32KState):
+    dtype = np.float64
+
+
+def _run_velocity(fn, state_cls, prob, state, t0, nsteps, record_every, nthreads):
+    state = state or state_cls(prob)
     nsteps = prob.src.size - t0 if nsteps is None else nsteps
     nrec = (t0 + nsteps) // record_every - t0 // record_every if record_every > 0 else 0
-    surf = np.zeros((max(nrec, 0), prob.nx, prob.ny), np.float32)
+    surf = np.zeros((max(nrec, 0), prob.nx, prob.ny), state_cls.dtype)
     st = state._c()
-    rc = lib().ora_f32k_run(ctypes.byref(prob.p), ctypes.byref(st), t0, nsteps, record_every,
+    rc = getattr(lib(), fn)(ctypes.byref(prob.p), ctypes.byref(st), t0, nsteps, record_every,
                             surf.ctypes.data if nrec > 0 else None, nthreads)
     if rc != 0:
-        raise ValueError(f"oracle f32k run failed: {rc}")
+        raise ValueError(f"oracle {fn} failed: {rc}")
     return state, surf
+
+
+def run_f32k(prob: OracleProblem, state: F32KState | None = None, t0=0, nsteps=None, record_every=0,
+             nthreads=0):
+    """FP32 velocity form with Kahan-compensated u (the GPU F32K scheme)."""
+    return _run_velocity("ora_run_f32k", F32KState, prob, state, t0, nsteps, record_every, nthreads)
+
+
+def run_f64v(prob: OracleProblem, state: F64VState | None = None, t0=0, nsteps=None, record_every=0,
+             nthreads=0):
+    """The same velocity-form scheme in FP64 (the GPU F64V scheme)."""
+    return _run_velocity("ora_run_f64v", F64VState, prob, state, t0, nsteps, record_every, nthreads)

@@ -422,278 +422,6 @@ int ora_f64_run(const ora_problem *p, ora_f64_state *s, int t0, int nsteps, int 
     return 0;
 }
 
-/* ------------------------------------------------------------------------ */
-/* (2) FP32 velocity form with Kahan-compensated displacement                */
-/* ------------------------------------------------------------------------ */
-/*
- * Per-material float constants: C (12) rounded from double, and
- * dtr = (float)(dt / P).  Spacings enter as float reciprocals
- * (float)(1.0 / d).  With e* strains and d* differences:
- *   T1 = fmaf(C00, e1, fmaf(C01, e2, C02 * e3))       (T2, T3 alike)
- *   T4 = C33 * fmaf(duy_dz, ifdz, duz_dy * ifdy)        (T5, T6 alike)
- *   div_x = fmaf(dT1, ifdx, fmaf(dT6, isdy, dT5 * isdz))  (div_y, div_z alike)
- *   v' = fmaf(dtr, div, v);  y = fmaf(dt, v', -c);  t = u + y;
- *   c' = (t - u) - y;  u' = t
- * Faces: u'[b] = fmaf(coef, V - u[b], u[b -/+ 1]) with V the value of the
- * inner neighbour after the earlier faces; v' = c' = 0 there.  Points that the
- * reference never writes keep u, v and c.
- */
-
-typedef struct {
-    float *ux, *uy, *uz;
-    float *vx, *vy, *vz;
-    float *cx, *cy, *cz;
-} ora_f32k_state;
-
-typedef struct {
-    float c[12];
-    float dtr;
-} f32mat;
-
-typedef struct {
-    float *fdx, *fdy, *fdz, *sdx, *sdy, *sdz; /* reciprocals */
-    float fdx0, fdy0, fdz0, sdx0, sdy0, sdz0;
-    f32mat *mt;
-    float dt;
-    float abc[8];
-} f32consts;
-
-static void f32_consts(const ora_problem *p, f32consts *k) {
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    k->fdx = (float *)malloc(sizeof(float) * (nx - 1));
-    k->fdy = (float *)malloc(sizeof(float) * (ny - 1));
-    k->fdz = (float *)malloc(sizeof(float) * (nz - 1));
-    k->sdx = (float *)malloc(sizeof(float) * (nx - 2));
-    k->sdy = (float *)malloc(sizeof(float) * (ny - 2));
-    k->sdz = (float *)malloc(sizeof(float) * (nz - 2));
-    for (int i = 0; i < nx - 1; i++) k->fdx[i] = (float)(1.0 / p->fdx[i]);
-    for (int i = 0; i < ny - 1; i++) k->fdy[i] = (float)(1.0 / p->fdy[i]);
-    for (int i = 0; i < nz - 1; i++) k->fdz[i] = (float)(1.0 / p->fdz[i]);
-    for (int i = 0; i < nx - 2; i++) k->sdx[i] = (float)(1.0 / p->sdx[i]);
-    for (int i = 0; i < ny - 2; i++) k->sdy[i] = (float)(1.0 / p->sdy[i]);
-    for (int i = 0; i < nz - 2; i++) k->sdz[i] = (float)(1.0 / p->sdz[i]);
-    k->fdx0 = k->fdx[0]; k->fdy0 = k->fdy[0]; k->fdz0 = k->fdz[0];
-    k->sdx0 = k->sdx[0]; k->sdy0 = k->sdy[0]; k->sdz0 = k->sdz[0];
-    k->mt = (f32mat *)malloc(sizeof(f32mat) * p->nmat);
-    for (int m = 0; m < p->nmat; m++) {
-        const double *t = p->table + (size_t)m * ORA_NTAB;
-        for (int q = 0; q < 12; q++) k->mt[m].c[q] = (float)t[q];
-        k->mt[m].dtr = (float)(p->dt / t[12]);
-    }
-    k->dt = (float)p->dt;
-    double c[8];
-    ora_abc_coeffs(p, c);
-    for (int q = 0; q < 8; q++) k->abc[q] = p->bc == 1 ? 0.0f : (float)c[q];
-}
-
-static void f32_consts_free(f32consts *k) {
-    free(k->fdx); free(k->fdy); free(k->fdz); free(k->sdx); free(k->sdy); free(k->sdz); free(k->mt);
-}
-
-typedef struct {
-    float *T1, *T2, *T3, *T4, *T5, *T6;
-} f32stress;
-
-/* u read with the source substituted on the x=0 plane of uz */
-static inline float uzs(const ora_problem *p, const float *uz, float s, int i, int j, int k) {
-    if (i == 0 && (p->source_mode == 1 || k == 0)) return s;
-    return uz[I3(p->ny, p->nz - 1, i, j, k)];
-}
-
-static void f32_stress(const ora_problem *p, const f32consts *K, const ora_f32k_state *s, float src, f32stress *T) {
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    const float *ux = s->ux, *uy = s->uy, *uz = s->uz;
-    const uint8_t *mat = p->mat;
-#pragma omp parallel for schedule(static)
-    for (int i = 1; i <= nx - 2; i++)
-        for (int j = 1; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                const float *c = K->mt[mat[I3(ny, nz, i, j, k)]].c;
-                float dux = ux[I3(ny, nz, i, j, k)] - ux[I3(ny, nz, i - 1, j, k)];
-                float duy = uy[I3(ny - 1, nz, i, j, k)] - uy[I3(ny - 1, nz, i, j - 1, k)];
-                float e1, e2, e3;
-                if (k == 0) {
-                    float duz = uzs(p, uz, src, i, j, 0);
-                    e1 = dux * K->sdx0; e2 = duy * K->sdy0; e3 = duz * K->sdz0;
-                } else {
-                    float duz = uzs(p, uz, src, i, j, k) - uzs(p, uz, src, i, j, k - 1);
-                    e1 = dux * K->sdx[i - 1]; e2 = duy * K->sdy[j - 1]; e3 = duz * K->sdz[k - 1];
-                }
-                size_t o = I3(ny, nz, i, j, k);
-                T->T1[o] = fmaf(c[0], e1, fmaf(c[1], e2, c[2] * e3));
-                T->T2[o] = fmaf(c[3], e1, fmaf(c[4], e2, c[5] * e3));
-                T->T3[o] = k == 0 ? 0.0f : fmaf(c[6], e1, fmaf(c[7], e2, c[8] * e3));
-            }
-#pragma omp parallel for schedule(static)
-    for (int i = 1; i <= nx - 2; i++)
-        for (int j = 0; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float a = uy[I3(ny - 1, nz, i, j, k + 1)] - uy[I3(ny - 1, nz, i, j, k)];
-                float b = uzs(p, uz, src, i, j + 1, k) - uzs(p, uz, src, i, j, k);
-                float v;
-                if (k == 0) v = K->mt[mat[I3(ny, nz, i, j + 1, 0)]].c[9] * fmaf(a, K->fdy0, b * K->fdz0);
-                else v = K->mt[mat[I3(ny, nz, i, j + 1, k + 1)]].c[9] * fmaf(a, K->fdz[k], b * K->fdy[j]);
-                T->T4[I3(ny - 1, nz - 1, i, j, k)] = v;
-            }
-#pragma omp parallel for schedule(static)
-    for (int i = 0; i <= nx - 2; i++)
-        for (int j = 1; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float a = ux[I3(ny, nz, i, j, k + 1)] - ux[I3(ny, nz, i, j, k)];
-                float b = uzs(p, uz, src, i + 1, j, k) - uzs(p, uz, src, i, j, k);
-                float v;
-                if (k == 0) v = K->mt[mat[I3(ny, nz, i + 1, j, 0)]].c[10] * fmaf(a, K->fdx0, b * K->fdz0);
-                else v = K->mt[mat[I3(ny, nz, i + 1, j, k + 1)]].c[10] * fmaf(a, K->fdz[k], b * K->fdx[i]);
-                T->T5[I3(ny, nz - 1, i, j, k)] = v;
-            }
-#pragma omp parallel for schedule(static)
-    for (int i = 0; i <= nx - 2; i++)
-        for (int j = 0; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float a = ux[I3(ny, nz, i, j + 1, k)] - ux[I3(ny, nz, i, j, k)];
-                float b = uy[I3(ny - 1, nz, i + 1, j, k)] - uy[I3(ny - 1, nz, i, j, k)];
-                float v;
-                if (k == 0) v = K->mt[mat[I3(ny, nz, i + 1, j + 1, 0)]].c[11] * fmaf(a, K->fdx0, b * K->fdz0);
-                else v = K->mt[mat[I3(ny, nz, i + 1, j + 1, k)]].c[11] * fmaf(a, K->fdy[j], b * K->fdx[i]);
-                T->T6[I3(ny - 1, nz, i, j, k)] = v;
-            }
-}
-
-static inline void kahan(float u, float v, float c, float dtr, float div, float dt, float *u2, float *v2, float *c2) {
-    float vn = fmaf(dtr, div, v);
-    float y = fmaf(dt, vn, -c);
-    float t = u + y;
-    *c2 = (t - u) - y;
-    *v2 = vn;
-    *u2 = t;
-}
-
-static void f32_update(const ora_problem *p, const f32consts *K, const ora_f32k_state *s, ora_f32k_state *o,
-                       const f32stress *T) {
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    const uint8_t *mat = p->mat;
-    const float dt = K->dt;
-#pragma omp parallel for schedule(static)
-    for (int i = 0; i <= nx - 2; i++)
-        for (int j = 1; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float d1 = T->T1[I3(ny, nz, i + 1, j, k)] - T->T1[I3(ny, nz, i, j, k)];
-                float d6 = T->T6[I3(ny - 1, nz, i, j, k)] - T->T6[I3(ny - 1, nz, i, j - 1, k)];
-                float div, dtr;
-                if (k == 0) {
-                    float d5 = T->T5[I3(ny, nz - 1, i, j, 0)];
-                    div = fmaf(d1, K->fdx0, fmaf(d6, K->sdy0, d5 * K->sdz0));
-                    dtr = K->mt[mat[I3(ny, nz, i + 1, j, 0)]].dtr;
-                } else {
-                    float d5 = T->T5[I3(ny, nz - 1, i, j, k)] - T->T5[I3(ny, nz - 1, i, j, k - 1)];
-                    div = fmaf(d1, K->fdx[i], fmaf(d6, K->sdy[j - 1], d5 * K->sdz[k - 1]));
-                    dtr = K->mt[mat[I3(ny, nz, i + 1, j, k)]].dtr;
-                }
-                size_t q = I3(ny, nz, i, j, k);
-                kahan(s->ux[q], s->vx[q], s->cx[q], dtr, div, dt, &o->ux[q], &o->vx[q], &o->cx[q]);
-            }
-#pragma omp parallel for schedule(static)
-    for (int i = 1; i <= nx - 2; i++)
-        for (int j = 0; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float d6 = T->T6[I3(ny - 1, nz, i, j, k)] - T->T6[I3(ny - 1, nz, i - 1, j, k)];
-                float d2 = T->T2[I3(ny, nz, i, j + 1, k)] - T->T2[I3(ny, nz, i, j, k)];
-                float div, dtr;
-                if (k == 0) {
-                    float d4 = T->T4[I3(ny - 1, nz - 1, i, j, 0)];
-                    div = fmaf(d6, K->sdx0, fmaf(d2, K->fdy0, d4 * K->sdz0));
-                    dtr = K->mt[mat[I3(ny, nz, i, j + 1, 0)]].dtr;
-                } else {
-                    float d4 = T->T4[I3(ny - 1, nz - 1, i, j, k)] - T->T4[I3(ny - 1, nz - 1, i, j, k - 1)];
-                    div = fmaf(d6, K->sdx[i - 1], fmaf(d2, K->fdy[j], d4 * K->sdz[k - 1]));
-                    dtr = K->mt[mat[I3(ny, nz, i, j + 1, k)]].dtr;
-                }
-                size_t q = I3(ny - 1, nz, i, j, k);
-                kahan(s->uy[q], s->vy[q], s->cy[q], dtr, div, dt, &o->uy[q], &o->vy[q], &o->cy[q]);
-            }
-#pragma omp parallel for schedule(static)
-    for (int i = 1; i <= nx - 2; i++)
-        for (int j = 1; j <= ny - 2; j++)
-            for (int k = 0; k <= nz - 2; k++) {
-                float d5 = T->T5[I3(ny, nz - 1, i, j, k)] - T->T5[I3(ny, nz - 1, i - 1, j, k)];
-                float d4 = T->T4[I3(ny - 1, nz - 1, i, j, k)] - T->T4[I3(ny - 1, nz - 1, i, j - 1, k)];
-                float t3n = T->T3[I3(ny, nz, i, j, k + 1)];
-                float div, dtr;
-                if (k == 0) {
-                    if (p->surface_mode == 0) div = fmaf(d5, K->sdx0, d4 * K->sdy0) + t3n;
-                    else div = fmaf(d5, K->sdx0, fmaf(d4, K->sdy0, t3n * K->fdz0));
-                    dtr = K->mt[mat[I3(ny, nz, i, j, 0)]].dtr;
-                } else {
-                    float d3 = t3n - T->T3[I3(ny, nz, i, j, k)];
-                    div = fmaf(d5, K->sdx[i - 1], fmaf(d4, K->sdy[j - 1], d3 * K->fdz[k]));
-                    dtr = K->mt[mat[I3(ny, nz, i, j, k + 1)]].dtr;
-                }
-                size_t q = I3(ny, nz - 1, i, j, k);
-                kahan(s->uz[q], s->vz[q], s->cz[q], dtr, div, dt, &o->uz[q], &o->vz[q], &o->cz[q]);
-            }
-}
-
-/* f32 faces: o holds the new state with every non-face point already final. */
-static void f32_faces(const ora_problem *p, const f32consts *K, const ora_f32k_state *s, ora_f32k_state *o,
-                      float src) {
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    const float *ux = s->ux, *uy = s->uy, *uz = s->uz;
-    float *xn = o->ux, *yn = o->uy, *zn = o->uz;
-    const float *c = K->abc;
-    const int rigid = p->bc == 1;
-#define F32ABC(dst, nbr_new, nbr_old, self_old, coef) \
-    (dst) = rigid ? 0.0f : fmaf((coef), (nbr_new) - (self_old), (nbr_old))
-    for (int j = 0; j < ny; j++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(xn[I3(ny, nz, nx - 2, j, k)], xn[I3(ny, nz, nx - 3, j, k)], ux[I3(ny, nz, nx - 3, j, k)],
-                   ux[I3(ny, nz, nx - 2, j, k)], c[0]);
-    for (int j = 0; j < ny - 1; j++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(yn[I3(ny - 1, nz, nx - 1, j, k)], yn[I3(ny - 1, nz, nx - 2, j, k)],
-                   uy[I3(ny - 1, nz, nx - 2, j, k)], uy[I3(ny - 1, nz, nx - 1, j, k)], c[1]);
-    for (int j = 0; j < ny; j++)
-        for (int k = 0; k < nz - 1; k++)
-            F32ABC(zn[I3(ny, nz - 1, nx - 1, j, k)], zn[I3(ny, nz - 1, nx - 2, j, k)],
-                   uzs(p, uz, src, nx - 2, j, k), uzs(p, uz, src, nx - 1, j, k), c[1]);
-    for (int i = 0; i < nx - 1; i++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(xn[I3(ny, nz, i, 0, k)], xn[I3(ny, nz, i, 1, k)], ux[I3(ny, nz, i, 1, k)], ux[I3(ny, nz, i, 0, k)],
-                   c[2]);
-    for (int i = 0; i < nx; i++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(yn[I3(ny - 1, nz, i, 0, k)], yn[I3(ny - 1, nz, i, 1, k)], uy[I3(ny - 1, nz, i, 1, k)],
-                   uy[I3(ny - 1, nz, i, 0, k)], c[3]);
-    for (int i = 0; i < nx; i++)
-        for (int k = 0; k < nz - 1; k++)
-            F32ABC(zn[I3(ny, nz - 1, i, 0, k)], zn[I3(ny, nz - 1, i, 1, k)], uzs(p, uz, src, i, 1, k),
-                   uzs(p, uz, src, i, 0, k), c[2]);
-    for (int i = 0; i < nx - 1; i++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(xn[I3(ny, nz, i, ny - 1, k)], xn[I3(ny, nz, i, ny - 2, k)], ux[I3(ny, nz, i, ny - 2, k)],
-                   ux[I3(ny, nz, i, ny - 1, k)], c[4]);
-    for (int i = 0; i < nx; i++)
-        for (int k = 0; k < nz; k++)
-            F32ABC(yn[I3(ny - 1, nz, i, ny - 2, k)], yn[I3(ny - 1, nz, i, ny - 3, k)],
-                   uy[I3(ny - 1, nz, i, ny - 3, k)], uy[I3(ny - 1, nz, i, ny - 2, k)], c[5]);
-    for (int i = 0; i < nx; i++)
-        for (int k = 0; k < nz - 1; k++)
-            F32ABC(zn[I3(ny, nz - 1, i, ny - 1, k)], zn[I3(ny, nz - 1, i, ny - 2, k)],
-                   uzs(p, uz, src, i, ny - 2, k), uzs(p, uz, src, i, ny - 1, k), c[4]);
-    for (int i = 0; i < nx - 1; i++)
-        for (int j = 0; j < ny; j++)
-            F32ABC(xn[I3(ny, nz, i, j, nz - 1)], xn[I3(ny, nz, i, j, nz - 2)], ux[I3(ny, nz, i, j, nz - 2)],
-                   ux[I3(ny, nz, i, j, nz - 1)], c[6]);
-    for (int i = 0; i < nx; i++)
-        for (int j = 0; j < ny - 1; j++)
-            F32ABC(yn[I3(ny - 1, nz, i, j, nz - 1)], yn[I3(ny - 1, nz, i, j, nz - 2)],
-                   uy[I3(ny - 1, nz, i, j, nz - 2)], uy[I3(ny - 1, nz, i, j, nz - 1)], c[6]);
-    for (int i = 0; i < nx; i++)
-        for (int j = 0; j < ny; j++)
-            F32ABC(zn[I3(ny, nz - 1, i, j, nz - 2)], zn[I3(ny, nz - 1, i, j, nz - 3)],
-                   uzs(p, uz, src, i, j, nz - 3), uzs(p, uz, src, i, j, nz - 2), c[7]);
-#undef F32ABC
-}
-
 /* face predicates of the reference's four absorbing faces */
 static inline int on_face_x(const ora_problem *p, int comp, int i) { return i == (comp == 0 ? p->nx - 2 : p->nx - 1); }
 static inline int on_face_y(const ora_problem *p, int comp, int j) {
@@ -701,63 +429,22 @@ static inline int on_face_y(const ora_problem *p, int comp, int j) {
 }
 static inline int on_face_z(const ora_problem *p, int comp, int k) { return k == (comp == 2 ? p->nz - 2 : p->nz - 1); }
 
-static void f32_zero_faces_vc(const ora_problem *p, ora_f32k_state *o) {
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    for (int comp = 0; comp < 3; comp++) {
-        int ex = nx - (comp == 0), ey = ny - (comp == 1), ez = nz - (comp == 2);
-        float *v = comp == 0 ? o->vx : comp == 1 ? o->vy : o->vz;
-        float *c = comp == 0 ? o->cx : comp == 1 ? o->cy : o->cz;
-        for (int i = 0; i < ex; i++)
-            for (int j = 0; j < ey; j++)
-                for (int k = 0; k < ez; k++)
-                    if (on_face_x(p, comp, i) || on_face_y(p, comp, j) || on_face_z(p, comp, k)) {
-                        v[I3(ey, ez, i, j, k)] = 0.0f;
-                        c[I3(ey, ez, i, j, k)] = 0.0f;
-                    }
-    }
-}
 
-int ora_f32k_run(const ora_problem *p, ora_f32k_state *s, int t0, int nsteps, int record_every, float *surf,
-                 int nthreads) {
-    int rc = check_problem(p);
-    if (rc) return rc;
-    if (t0 < 0 || t0 + nsteps > p->nsrc) return -5;
-    set_threads(nthreads);
-    const int nx = p->nx, ny = p->ny, nz = p->nz;
-    size_t n123 = (size_t)nx * ny * nz;
-    size_t nux = (size_t)(nx - 1) * ny * nz, nuy = (size_t)nx * (ny - 1) * nz, nuz = (size_t)nx * ny * (nz - 1);
-    f32consts K;
-    f32_consts(p, &K);
-    f32stress T;
-    T.T1 = (float *)calloc(n123, sizeof(float));
-    T.T2 = (float *)calloc(n123, sizeof(float));
-    T.T3 = (float *)calloc(n123, sizeof(float));
-    T.T4 = (float *)calloc((size_t)nx * (ny - 1) * (nz - 1), sizeof(float));
-    T.T5 = (float *)calloc((size_t)(nx - 1) * ny * (nz - 1), sizeof(float));
-    T.T6 = (float *)calloc((size_t)(nx - 1) * (ny - 1) * nz, sizeof(float));
-    ora_f32k_state o;
-    size_t sz[3] = {nux, nuy, nuz};
-    float **dst[9] = {&o.ux, &o.uy, &o.uz, &o.vx, &o.vy, &o.vz, &o.cx, &o.cy, &o.cz};
-    float *srcp[9] = {s->ux, s->uy, s->uz, s->vx, s->vy, s->vz, s->cx, s->cy, s->cz};
-    for (int q = 0; q < 9; q++) *dst[q] = (float *)malloc(sz[q % 3] * sizeof(float));
-    int first_record = record_every > 0 ? t0 / record_every : 0;
-    for (int tt = t0; tt < t0 + nsteps; tt++) {
-        float src = (float)p->src[tt];
-        /* stale copy: points the reference never writes keep their state */
-        for (int q = 0; q < 9; q++) memcpy(*dst[q], srcp[q], sz[q % 3] * sizeof(float));
-        f32_stress(p, &K, s, src, &T);
-        f32_update(p, &K, s, &o, &T);
-        f32_faces(p, &K, s, &o, src);
-        f32_zero_faces_vc(p, &o);
-        for (int q = 0; q < 9; q++) memcpy(srcp[q], *dst[q], sz[q % 3] * sizeof(float));
-        if (record_every > 0 && surf && (tt + 1) % record_every == 0) {
-            float *d = surf + (size_t)((tt + 1) / record_every - 1 - first_record) * nx * ny;
-            for (int i = 0; i < nx; i++)
-                for (int j = 0; j < ny; j++) d[(size_t)i * ny + j] = s->uz[I3(ny, nz - 1, i, j, 0)];
-        }
-    }
-    for (int q = 0; q < 9; q++) free(*dst[q]);
-    free(T.T1); free(T.T2); free(T.T3); free(T.T4); free(T.T5); free(T.T6);
-    f32_consts_free(&K);
-    return 0;
-}
+/* ------------------------------------------------------------------------ */
+/* (2) velocity form with Kahan-compensated displacement: FP32 and FP64      */
+/* ------------------------------------------------------------------------ */
+#define REAL float
+#define FMA fmaf
+#define V(name) name##_f32k
+#include "velocity_form.inc"
+#undef REAL
+#undef FMA
+#undef V
+
+#define REAL double
+#define FMA fma
+#define V(name) name##_f64v
+#include "velocity_form.inc"
+#undef REAL
+#undef FMA
+#undef V

@@ -14,7 +14,7 @@ PHONO_OK = 0
 ERRORS = {-1: "PHONO_ERR_ARG", -2: "PHONO_ERR_CUDA", -3: "PHONO_ERR_NOMEM", -4: "PHONO_ERR_STATE",
           -5: "PHONO_ERR_NUMERIC"}
 
-PRECISIONS = {"f64": 0, "f32k": 1}
+PRECISIONS = {"f64": 0, "f32k": 1, "f64v": 2}
 SURFACE_MODES = {"reference": 0, "corrected": 1}
 BCS = {"absorbing": 0, "reference": 0, "rigid": 1}
 SOURCE_MODES = {"line": 0, "wall": 1}

@@ -14,6 +14,8 @@ cudaError_t configure_step_f64(int tj);
 cudaError_t configure_step_f32k(int tj);
 cudaError_t launch_step_f64(const StepArgs<double>& a, int tj, int n_face_blocks, cudaStream_t st);
 cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int n_face_blocks, cudaStream_t st);
+cudaError_t configure_step_f64v(int tj);
+cudaError_t launch_step_f64v(const StepArgs<double>& a, int tj, int n_face_blocks, cudaStream_t st);
 cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st);
 
 __global__ void advance_step_kernel(int* p, int n) { *p += n; }
@@ -146,11 +148,13 @@ static int upload_materials(phono_handle* h, const uint8_t* mat, const double* t
   const double dt = h->d.dt;
   const double dt2 = dt * dt;
   if (h->es == 8) {
+    const bool leapfrog = h->d.precision == PHONO_F64;
     std::vector<double> t(16 * nmat, 0.0);
     for (int m = 0; m < nmat; m++) {
       const double* row = table + m * PHONO_TABLE_COLS;
       for (int q = 0; q < 12; q++) t[m * 16 + q] = row[q];
-      t[m * 16 + 12] = dt2 / row[12];  // (dt**2 / P) of base_solver.py:443
+      // (dt**2 / P) of base_solver.py:443 for the leapfrog, dt / P for the velocity form
+      t[m * 16 + 12] = leapfrog ? dt2 / row[12] : dt / row[12];
       t[m * 16 + 13] = row[12];
       t[m * 16 + 14] = dt;
     }
@@ -186,7 +190,9 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.sp.sdy = (const R*)h->sp[4];
   a.sp.sdz = (const R*)h->sp[5];
   R s0[6];
-  for (int q = 0; q < 6; q++) s0[q] = sizeof(R) == 8 ? (R)h->h_sp0[q] : (R)(1.0 / h->h_sp0[q]);
+  // the leapfrog divides by raw spacings; the velocity forms multiply by reciprocals
+  const bool raw = h->d.precision == PHONO_F64;
+  for (int q = 0; q < 6; q++) s0[q] = raw ? (R)h->h_sp0[q] : (R)(1.0 / h->h_sp0[q]);
   a.sp.fdx0 = s0[0];
   a.sp.fdy0 = s0[1];
   a.sp.fdz0 = s0[2];
@@ -225,6 +231,8 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
 static cudaError_t launch_one(phono_handle* h, int step_off) {
   if (h->d.precision == PHONO_F64)
     return launch_step_f64(make_args<double>(h, step_off), h->tj, h->separate_faces, h->stream);
+  if (h->d.precision == PHONO_F64V)
+    return launch_step_f64v(make_args<double>(h, step_off), h->tj, h->separate_faces, h->stream);
   return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->separate_faces, h->stream);
 }
 
@@ -235,7 +243,8 @@ static int check_desc(const phono_desc* d) {
   if (!d->fdx || !d->fdy || !d->fdz || !d->sdx || !d->sdy || !d->sdz) return fail(PHONO_ERR_ARG, "spacing array is NULL");
   if (!d->mat || !d->table) return fail(PHONO_ERR_ARG, "material ids or table is NULL");
   if (d->nmat < 1 || d->nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
-  if (d->precision != PHONO_F64 && d->precision != PHONO_F32K) return fail(PHONO_ERR_ARG, "unknown precision");
+  if (d->precision != PHONO_F64 && d->precision != PHONO_F32K && d->precision != PHONO_F64V)
+    return fail(PHONO_ERR_ARG, "unknown precision");
   if (d->surface_mode < 0 || d->surface_mode > 1) return fail(PHONO_ERR_ARG, "unknown surface_mode");
   if (d->bc < 0 || d->bc > 1) return fail(PHONO_ERR_ARG, "unknown bc");
   if (d->source_mode < 0 || d->source_mode > 1) return fail(PHONO_ERR_ARG, "unknown source_mode");
@@ -350,11 +359,11 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->d.fdx = h->d.fdy = h->d.fdz = h->d.sdx = h->d.sdy = h->d.sdz = nullptr;
   h->d.mat = nullptr;
   h->d.table = nullptr;
-  const bool f64 = d->precision == PHONO_F64;
-  h->es = f64 ? 8 : 4;
+  const bool f64 = d->precision == PHONO_F64;  // leapfrog state (u_old, u, u_new)
+  h->es = d->precision == PHONO_F32K ? 4 : 8;
   const int nx = d->nx, ny = d->ny, nz = d->nz;
   // padded layout: planes -1..nx, rows -1..ny, 32-byte front pad in z
-  const long long koff = f64 ? Lay<double>::KOFF : Lay<float>::KOFF;
+  const long long koff = h->es == 8 ? Lay<double>::KOFF : Lay<float>::KOFF;
   const long long pz = round_up(koff + nz + 1, 128 / h->es);
   h->nbuf = f64 ? 3 : 2;
   h->g.nx = nx;
@@ -424,7 +433,8 @@ int phono_create(const phono_desc* d, phono_handle** out) {
       return fail(PHONO_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
     }                                                                                   \
   } while (0)
-  TRYC(f64 ? configure_step_f64(h->tj) : configure_step_f32k(h->tj));
+  TRYC(f64 ? configure_step_f64(h->tj)
+           : (d->precision == PHONO_F64V ? configure_step_f64v(h->tj) : configure_step_f32k(h->tj)));
   TRYC(cudaEventCreate(&h->ev0));
   TRYC(cudaEventCreate(&h->ev1));
   const size_t fb = h->field_elems * h->es * 3 * h->nbuf;
@@ -448,6 +458,10 @@ int phono_create(const phono_desc* d, phono_handle** out) {
     TRYC(cudaMemcpy(h->sp64[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
     if (f64) {
       TRYC(cudaMemcpy(h->sp[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    } else if (h->es == 8) {  // F64V: reciprocals in double
+      std::vector<double> r(lens[a]);
+      for (int q = 0; q < lens[a]; q++) r[q] = 1.0 / arrs[a][q];
+      TRYC(cudaMemcpy(h->sp[a], r.data(), (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
     } else {
       std::vector<float> r(lens[a]);
       for (int q = 0; q < lens[a]; q++) r[q] = (float)(1.0 / arrs[a][q]);
@@ -611,7 +625,8 @@ int phono_energy(phono_handle* h, double out[2]) {
   a.vx = field_ptr(h, f64 ? PHONO_FIELD_UX_OLD : PHONO_FIELD_VX);
   a.vy = field_ptr(h, f64 ? PHONO_FIELD_UY_OLD : PHONO_FIELD_VY);
   a.vz = field_ptr(h, f64 ? PHONO_FIELD_UZ_OLD : PHONO_FIELD_VZ);
-  a.f32 = f64 ? 0 : 1;
+  a.f32 = h->es == 4 ? 1 : 0;
+  a.vgiven = f64 ? 0 : 1;
   a.inv_dt = 1.0 / h->d.dt;
   a.fdx = h->sp64[0];
   a.fdy = h->sp64[1];

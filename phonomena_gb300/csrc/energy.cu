@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(EN_THREADS) energy_partial_kernel(EnergyArgs a
     };
     auto vel = [&](const void* u, const void* v) {
       double x = ld(v, a.f32, off);
-      return a.f32 ? x : (ld(u, 0, off) - x) * a.inv_dt;
+      return a.vgiven ? x : (ld(u, 0, off) - x) * a.inv_dt;
     };
     // kinetic energy at the interior displacement points, absorbing faces excluded
     if (i <= g.nx - 3 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_d
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int i = blockIdx.x;
   const int f32 = a.precision == PHONO_F32K;
+  const int vgiven = a.precision != PHONO_F64;
   const double inv_dt = 1.0 / a.dt;
   auto ix = [&](int ii, int jj, int kk) { return ((long long)ii * ny + jj) * nz + kk; };          // ux, mat
   auto iy = [&](int ii, int jj, int kk) { return ((long long)ii * (ny - 1) + jj) * nz + kk; };    // uy
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_d
   auto C = [&](int ii, int jj, int kk, int e) { return a.table[a.mat[ix(ii, jj, kk)] * 13 + e]; };
   auto vel = [&](const void* u, const void* v, long long off) {
     double x = ld(v, f32, off);
-    return f32 ? x : (ld(u, 0, off) - x) * inv_dt;
+    return vgiven ? x : (ld(u, 0, off) - x) * inv_dt;
   };
   double ek = 0.0, es = 0.0;
   for (int q = threadIdx.x; q < ny * nz; q += EN_THREADS) {
@@ -241,7 +242,8 @@ extern "C" int phono_energy_static(const phono_energy_dense* in, double* out_dev
   if (in->nx > PHONO_ENERGY_STATIC_MAX_NX)
     return fail(PHONO_ERR_ARG, "nx exceeds PHONO_ENERGY_STATIC_MAX_NX, the planes of the static scratch array");
   if ((long long)in->ny * in->nz > 0x7fffffffLL) return fail(PHONO_ERR_ARG, "ny * nz too large");
-  if (in->precision != PHONO_F64 && in->precision != PHONO_F32K) return fail(PHONO_ERR_ARG, "unknown precision");
+  if (in->precision != PHONO_F64 && in->precision != PHONO_F32K && in->precision != PHONO_F64V)
+    return fail(PHONO_ERR_ARG, "unknown precision");
   if (!in->ux || !in->uy || !in->uz || !in->vx || !in->vy || !in->vz || !in->mat || !in->table || !in->fdx ||
       !in->fdy || !in->fdz || !in->sdx || !in->sdy || !in->sdz)
     return fail(PHONO_ERR_ARG, "NULL device pointer in the input");

@@ -105,7 +105,8 @@ struct EnergyArgs {
   Geo g;
   const void *ux, *uy, *uz;
   const void *vx, *vy, *vz;  // F32K: velocity arrays; F64: u_old arrays
-  int f32;                   // element type of the arrays above
+  int f32;                   // element type of the arrays above (float / double)
+  int vgiven;                // vx.. hold the velocity (velocity forms) rather than u_old
   double inv_dt;             // F64: 1/dt to form (u - u_old)/dt
   const double *fdx, *fdy, *fdz, *sdx, *sdy, *sdz;
   const uint8_t* mat;

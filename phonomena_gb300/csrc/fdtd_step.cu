@@ -84,6 +84,33 @@ struct F32K {
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __fmaf_rn(coef, __fsub_rn(nbr_new, self_old), nbr_old);
   }
+  __device__ __forceinline__ static R fma(R a, R b, R c) { return __fmaf_rn(a, b, c); }
+  __device__ __forceinline__ static R add(R a, R b) { return __fadd_rn(a, b); }
+};
+
+// The F32K scheme carried out in FP64: the fast FP64 reference for judging
+// the FP32 error (same operation sequence, double rounding).
+struct F64V {
+  using R = double;
+  static constexpr bool kahan = true;
+  __device__ __forceinline__ static R sub(R a, R b) { return __dsub_rn(a, b); }
+  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
+    return __fma_rn(c[0], __dmul_rn(d1, a), __fma_rn(c[1], __dmul_rn(d2, b), __dmul_rn(c[2], __dmul_rn(d3, d))));
+  }
+  __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
+    return __dmul_rn(cs, __fma_rn(d1, a, __dmul_rn(d2, b)));
+  }
+  __device__ __forceinline__ static R div3(R d1, R a, R d2, R b, R d3, R c) {
+    return __fma_rn(d1, a, __fma_rn(d2, b, __dmul_rn(d3, c)));
+  }
+  __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
+    return __dadd_rn(__fma_rn(d1, a, __dmul_rn(d2, b)), t31);
+  }
+  __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
+    return __fma_rn(coef, __dsub_rn(nbr_new, self_old), nbr_old);
+  }
+  __device__ __forceinline__ static R fma(R a, R b, R c) { return __fma_rn(a, b, c); }
+  __device__ __forceinline__ static R add(R a, R b) { return __dadd_rn(a, b); }
 };
 
 // ---------------------------------------------------------------------------
@@ -301,10 +328,10 @@ __device__ __forceinline__ typename S::R update_value(typename S::R u, Pw<typena
     vn = cn = 0;
     return __dadd_rn(__dsub_rn(__dmul_rn(2.0, u), pw.p0), __dmul_rn(row[12], dv));
   } else {
-    R v2 = __fmaf_rn(row[12], dv, pw.p0);         // row[12] = dt / P
-    R y = __fmaf_rn(row[14], v2, -pw.p1);          // row[14] = dt
-    R t = __fadd_rn(u, y);
-    cn = __fsub_rn(__fsub_rn(t, u), y);
+    R v2 = S::fma(row[12], dv, pw.p0);  // row[12] = dt / P
+    R y = S::fma(row[14], v2, -pw.p1);   // row[14] = dt
+    R t = S::add(u, y);
+    cn = S::sub(S::sub(t, u), y);
     vn = v2;
     return t;
   }
@@ -632,6 +659,10 @@ cudaError_t launch_step_f64(const StepArgs<double>& a, int tj, int nf, cudaStrea
 }
 cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int nf, cudaStream_t st) {
   return launch_step<F32K>(a, tj, nf, st);
+}
+cudaError_t configure_step_f64v(int tj) { return configure_step<F64V>(tj); }
+cudaError_t launch_step_f64v(const StepArgs<double>& a, int tj, int nf, cudaStream_t st) {
+  return launch_step<F64V>(a, tj, nf, st);
 }
 
 }  // namespace phono

@@ -47,7 +47,7 @@ class DeviceSimulation:
         self.precision = precision
         self.record_every = int(record_every)
         self.max_steps = int(max_steps)
-        self.dtype = np.float64 if precision == "f64" else np.float32
+        self.dtype = np.float32 if precision == "f32k" else np.float64
         d = _lib.PhonoDesc(
             self.nx, self.ny, self.nz,
             *(self._sp[k].ctypes.data for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")),

@@ -70,12 +70,14 @@ def _oracle_prob(oracle, d):
                                 surface_mode=SURF[m["surface_mode"]], bc=BC[m["bc"]])
 
 
+@pytest.mark.parametrize("precision", ["f32k", "f64v"])
 @pytest.mark.parametrize("name", G.CASES)
-def test_f32k_bit_exact_vs_oracle(gpu_lib, oracle, name):
+def test_velocity_form_bit_exact_vs_oracle(gpu_lib, oracle, name, precision):
     d = G.load(name)
     m = d["meta"]
-    st, surf = oracle.run_f32k(_oracle_prob(oracle, d), record_every=m["record_every"])
-    with device_sim(d, precision="f32k") as sim:
+    run = oracle.run_f32k if precision == "f32k" else oracle.run_f64v
+    st, surf = run(_oracle_prob(oracle, d), record_every=m["record_every"])
+    with device_sim(d, precision=precision) as sim:
         sim.step(m["steps"])
         sim.sync()
         for key, ref in zip(("ux", "uy", "uz"), st.u):
@@ -120,6 +122,22 @@ def test_f64_and_f32k_vs_oracle_multi_tile(gpu_lib, oracle, cells, tile_j):
         for key, ref in zip(("ux", "uy", "uz"), s32.u):
             assert np.array_equal(sim.download(key), ref), key
         assert np.array_equal(sim.read_surface(), surf32)
+
+
+def test_f64v_matches_reference_arithmetic(gpu_lib):
+    """The FP64 velocity form (the fast FP64 error reference) agrees with the
+    reference-arithmetic FP64 path to 1e-12 relative L2 over 500 steps."""
+    d = G.load("config1_void_corrected")
+    out = {}
+    for precision in ("f64", "f64v"):
+        with device_sim(d, precision=precision) as sim:
+            sim.step(d["meta"]["steps"])
+            sim.sync()
+            out[precision] = ([sim.download(k) for k in ("ux", "uy", "uz")], sim.read_surface())
+    num = sum(np.linalg.norm(a - b) ** 2 for a, b in zip(out["f64"][0], out["f64v"][0])) ** 0.5
+    den = sum(np.linalg.norm(a) ** 2 for a in out["f64"][0]) ** 0.5
+    assert num / den < 1e-12, num / den
+    assert np.linalg.norm(out["f64"][1] - out["f64v"][1]) / np.linalg.norm(out["f64"][1]) < 1e-12
 
 
 def test_wall_source_matches_oracle(gpu_lib, oracle):
