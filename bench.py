@@ -109,9 +109,12 @@ class ClockSampler:
                 "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
 
 
-def graph_launches(nsteps):
+def graph_launches(nsteps, separate_faces=True):
+    """Kernels launched by phono_step(nsteps): per step the tile pass and the
+    face pass, plus one step-counter update per 12-step graph and remainder."""
+    per = 2 if separate_faces else 1
     full, rem = divmod(nsteps, GRAPH_CHUNK)
-    return full * (GRAPH_CHUNK + 1) + rem + (1 if rem else 0)
+    return full * (per * GRAPH_CHUNK + 1) + per * rem + (1 if rem else 0)
 
 
 def workload(cells, seed, fdtd_steps):
@@ -219,7 +222,20 @@ def main():
     spec, g, m, src = workload(cells, rank, S)
     nodes = spec.n_nodes
     sp = g.spacing()
-    kw = dict(surface_mode="corrected", max_steps=S, record_every=10, tile_j=args.tile_j, x_segment=args.x_segment)
+    # tile shapes: the project autotuner (untimed, cached per mesh and device)
+    shapes = {}
+    for prec in ("f32k", "f64v", "f64"):
+        if args.tile_j:
+            shapes[prec] = (args.tile_j, args.x_segment)
+        else:
+            from phonomena_gb300 import autotune
+
+            cands = None if prec == "f32k" else [(tj, xs) for tj in (8, 16) for xs in (24, 32, 40)]
+            shapes[prec] = autotune.tune(sp, m.ids, m.table, m.dt, precision=prec, candidates=cands)
+
+    def kw(prec):
+        return dict(surface_mode="corrected", max_steps=S, record_every=10, tile_j=shapes[prec][0],
+                    x_segment=shapes[prec][1])
 
     def barrier():
         torch.cuda.synchronize()
@@ -234,7 +250,8 @@ def main():
         return float(t.item())
 
     # ---- FP32 Kahan: device-resident throughput ----
-    sim = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f32k", **kw)
+    sim = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f32k", **kw("f32k"))
+    separate_faces = g.y.size >= 4
     sim.set_source(src)
     stream = torch.cuda.ExternalStream(sim.stream_ptr)
     for _ in range(args.warmup):
@@ -265,29 +282,38 @@ def main():
     achieved = BYTES_PER_NODE * nodes / (launch_ms / 1e3) / 1e9
     tpn = traffic_per_node("fdtd_step_kernel_f32k")
 
-    # ---- plain FP64 on the same crystal (one full run) ----
-    sim64 = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f64", **kw)
-    sim64.set_source(src)
-    s64 = torch.cuda.ExternalStream(sim64.stream_ptr)
-    sim64.step(GRAPH_CHUNK)
-    sim64.sync()
-    sim64.reset()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(s64)
-    sim64.step(S)
-    f1.record(s64)
-    f1.synchronize()
-    sim64.sync()
-    ms64 = max_over_ranks(f0.elapsed_time(f1))
-    value64 = world * nodes * S / (ms64 / 1e3) / 1e9
-    surf64 = sim64.read_surface()
-    u64 = [sim64.download(k) for k in ("ux", "uy", "uz")]
-    e64 = sim64.energy()
-    rel_surf = float(np.linalg.norm(surf32 - surf64) / np.linalg.norm(surf64))
-    rel_u = float(math.sqrt(sum(np.linalg.norm(a - b) ** 2 for a, b in zip(u32, u64)))
-                  / math.sqrt(sum(np.linalg.norm(b) ** 2 for b in u64)))
-    rel_e = float(abs(sum(e32) - sum(e64)) / abs(sum(e64)))
-    sim64.close()
+    # ---- FP64 on the same crystal, one full run each: the reference
+    # arithmetic (plain FP64 path, bit-identical to phonomena) and the FP64
+    # velocity form (the same scheme as the FP32 path) ----
+    def run_fp64(prec):
+        s = DeviceSimulation(sp, m.ids, m.table, m.dt, precision=prec, **kw(prec))
+        s.set_source(src)
+        st = torch.cuda.ExternalStream(s.stream_ptr)
+        s.step(GRAPH_CHUNK)
+        s.sync()
+        s.reset()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        s.step(S)
+        f1.record(st)
+        f1.synchronize()
+        s.sync()
+        t = max_over_ranks(f0.elapsed_time(f1))
+        out = (t, world * nodes * S / (t / 1e3) / 1e9, s.read_surface(),
+               [s.download(k) for k in ("ux", "uy", "uz")], s.energy())
+        s.close()
+        return out
+
+    def errors(ref):
+        _, _, surf64, u64, e64 = ref
+        return {"rel_l2_surface_uz": float(np.linalg.norm(surf32 - surf64) / np.linalg.norm(surf64)),
+                "rel_l2_u": float(math.sqrt(sum(np.linalg.norm(a - b) ** 2 for a, b in zip(u32, u64)))
+                                  / math.sqrt(sum(np.linalg.norm(b) ** 2 for b in u64))),
+                "rel_energy": float(abs(sum(e32) - sum(e64)) / abs(sum(e64))), "fdtd_steps": S}
+
+    r64 = run_fp64("f64")
+    r64v = run_fp64("f64v")
+    ms64, value64 = r64[0], r64[1]
 
     # ---- e2e through the public API with pinned host buffers ----
     def pinned(shape, dtype):
@@ -343,18 +369,26 @@ def main():
                        "nodes": nodes, "fdtd_steps": S, "l2": "inputs larger than L2 (state 612 MB)",
                        "parallelism": f"replicas x{world}"},
             "fp64": {"value": round(value64, 4), "unit": "Gcell-updates/s", "fdtd_steps": S,
-                     "ms": round(ms64, 3), "speedup_f32k_over_f64": round(value / value64, 3)},
-            "error_vs_fp64": {"rel_l2_surface_uz": rel_surf, "rel_l2_u": rel_u, "rel_energy": rel_e,
-                              "fdtd_steps": S},
+                     "ms": round(ms64, 3), "speedup_f32k_over_f64": round(value / value64, 3),
+                     "arithmetic": "reference leapfrog, IEEE division, bit-identical to phonomena",
+                     "tile": list(shapes["f64"])},
+            "fp64_velocity_form": {"value": round(r64v[1], 4), "unit": "Gcell-updates/s", "ms": round(r64v[0], 3),
+                                   "speedup_f32k_over_f64v": round(value / r64v[1], 3),
+                                   "tile": list(shapes["f64v"])},
+            "error_vs_fp64": errors(r64),
+            "error_vs_fp64_velocity_form": errors(r64v),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
                          "traffic": (round(tpn * nodes) if tpn else None),
                          "algorithmic_bytes_per_launch": BYTES_PER_NODE * nodes,
-                         "avg_launch_ms": round(launch_ms, 5)},
+                         "avg_launch_ms": round(launch_ms, 5),
+                         "launch_timing": "one time step = tile pass + face pass (+1/12 counter update); "
+                                          "the whole step is charged to the stencil kernel"},
+            "tile": list(shapes["f32k"]),
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": graph_launches(S) * args.steps,
+            "gpu_launches": graph_launches(S, separate_faces) * args.steps,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -382,7 +382,7 @@ int phono_create(const phono_desc* d, phono_handle** out) {
 
   // tiles
   h->tj = d->tile_j ? d->tile_j : 8;
-  h->xseg = d->x_segment ? d->x_segment : 64;
+  h->xseg = d->x_segment ? d->x_segment : 32;
   h->ntj = (ny - 1 + h->tj - 1) / h->tj;
   h->ntk = (nz - 1 + TK - 1) / TK;
   h->nseg = (nx - 1 + h->xseg - 1) / h->xseg;
