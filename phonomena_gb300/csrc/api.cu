@@ -387,11 +387,13 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->ntk = (nz - 1 + TK - 1) / TK;
   h->nseg = (nx - 1 + h->xseg - 1) / h->xseg;
   long long ntile = (long long)h->ntj * h->ntk * h->nseg;
-  // faces: per component z=N (ex*ey), y=N and y=0 (ex*(ez-1)), x=N ((ey-2)*(ez-1))
+  // face points left to the face pass, per component: z=N only where it meets
+  // an x / y face (2*ex + ey-2; the tile pass writes the rest), y=N and y=0
+  // (ex*(ez-1)), x=N ((ey-2)*(ez-1))
   long long acc = 0;
   for (int c = 0; c < 3; c++) {
     long long ex = nx - (c == 0), ey = ny - (c == 1), ez = nz - (c == 2);
-    long long cnt[4] = {ex * ey, ex * (ez - 1), ex * (ez - 1), (ey - 2) * (ez - 1)};
+    long long cnt[4] = {2 * ex + (ey - 2), ex * (ez - 1), ex * (ez - 1), (ey - 2) * (ez - 1)};
     for (int p = 0; p < 4; p++) {
       h->faces.off[c * 4 + p] = (int)acc;
       acc += cnt[p];

@@ -67,7 +67,8 @@ struct Spacing {
 // Face-point enumeration: for component c and plane p (0 z=N, 1 y=N, 2 y=0,
 // 3 x=N), off[c*4+p] is the first flattened index; off[12] is the total.
 // Planes are disjoint (a point on several faces belongs to the first plane in
-// that order).
+// that order).  Plane 0 lists only the z=N points that also lie on an x or y
+// face: the tile pass writes the others.
 struct FaceTable {
   int off[13];
 };

@@ -78,8 +78,9 @@ struct F32K {
   __device__ __forceinline__ static R div3(R d1, R a, R d2, R b, R d3, R c) {
     return __fmaf_rn(d1, a, __fmaf_rn(d2, b, __fmul_rn(d3, c)));
   }
+  // reference-precedence z = 0 row: T3[..,1] as the third term with factor 1
   __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
-    return __fadd_rn(__fmaf_rn(d1, a, __fmul_rn(d2, b)), t31);
+    return div3(d1, a, d2, b, t31, 1.0f);
   }
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __fmaf_rn(coef, __fsub_rn(nbr_new, self_old), nbr_old);
@@ -104,7 +105,7 @@ struct F64V {
     return __fma_rn(d1, a, __fma_rn(d2, b, __dmul_rn(d3, c)));
   }
   __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
-    return __dadd_rn(__fma_rn(d1, a, __dmul_rn(d2, b)), t31);
+    return div3(d1, a, d2, b, t31, 1.0);
   }
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __fma_rn(coef, __dsub_rn(nbr_new, self_old), nbr_old);
@@ -347,13 +348,16 @@ __device__ __forceinline__ void store_point(const Roles<typename S::R>& r, int c
   }
 }
 
+// a point the reference does not write this step keeps its state; returns u
 template <class S>
-__device__ __forceinline__ void store_stale(const Roles<typename S::R>& r, int c, long long off) {
-  r.out(c)[off] = __ldg(r.cur(c) + off);
+__device__ __forceinline__ typename S::R store_stale(const Roles<typename S::R>& r, int c, long long off) {
+  const typename S::R u = __ldg(r.cur(c) + off);
+  r.out(c)[off] = u;
   if constexpr (S::kahan) {
     r.vout(c)[off] = __ldg(r.vin(c) + off);
     r.cout(c)[off] = __ldg(r.cin(c) + off);
   }
+  return u;
 }
 
 template <class R>
@@ -485,7 +489,12 @@ __device__ __forceinline__ void face_point(const StepArgs<typename S::R>& a, con
   const int c = q >> 2, pl = q & 3, rr = idx - a.faces.off[q];
   const int ex = ext_x(g, c), ey = ext_y(g, c), ez = ext_z(g, c);
   int i, j, k;
-  if (pl == 0) { i = rr / ey; j = rr - i * ey; k = ez - 1; }
+  if (pl == 0) {  // z = N points that are also on an x / y face (the rest: tile pass)
+    k = ez - 1;
+    if (rr < ex) { i = rr; j = 0; }
+    else if (rr < 2 * ex) { i = rr - ex; j = ey - 1; }
+    else { i = ex - 1; j = 1 + rr - 2 * ex; }
+  }
   else if (pl == 1) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = ey - 1; }
   else if (pl == 2) { i = rr / (ez - 1); k = rr - i * (ez - 1); j = 0; }
   else { j = rr / (ez - 1); k = rr - j * (ez - 1); j += 1; i = ex - 1; }

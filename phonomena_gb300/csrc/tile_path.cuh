@@ -68,12 +68,22 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
   const R fdy_j = j <= ny - 2 ? __ldg(a.sp.fdy + j) : R(1);
   const R sdz_m = k >= 1 && k <= nz - 2 ? __ldg(a.sp.sdz + k - 1) : R(1);
   const R fdz_k = k <= nz - 2 ? __ldg(a.sp.fdz + k) : R(1);
-  // spacings as used by the z = 0 row or the interior
+  // spacings as used by the z = 0 row or the interior (the x ones are per plane)
   const R t123_b = kz ? a.sp.sdy0 : sdy_m, t123_d = kz ? a.sp.sdz0 : sdz_m;
+  const R uy_b = kz ? a.sp.fdy0 : fdy_j, uy_c = kz ? a.sp.sdz0 : sdz_m;
+  const R uz_b = kz ? a.sp.sdy0 : sdy_m, uz_c = kz ? (a.surface_mode == 0 ? R(1) : a.sp.fdz0) : fdz_k;
+  const R ux_b = kz ? a.sp.sdy0 : sdy_m, ux_c = kz ? a.sp.sdz0 : sdz_m;
   // output classification (component extents, faces, V0 sets)
   const bool face_y = j == 0 || j == ny - 2;  // uy: y = 0 / y = N faces
   const bool face_z = j == 0 || k == nz - 2;  // uz: y = 0 / z = N faces
   const bool face_x = j == 0;                 // ux: y = 0 face (x = N checked per plane)
+  // The z = N face point above an (i, j) that is on no x / y face is one face
+  // formula applied to the value this thread computes at k = kz - 1
+  // (base_solver.py:552-554, applied last); the thread writes it.  Points on
+  // x / y faces as well are left to the face pass.
+  const bool zface_xy = k == nz - 2;  // ux, uy: z = N at k = nz-1 (ux: and not the x = N plane)
+  const bool zface_z = k == nz - 3;   // uz: z = N at k = nz-2
+  const bool rigid = a.bc == 1;
 
   // -------- TMA ring --------
   auto issue = [&](int p) {  // plane p into its ring slot (one thread)
@@ -121,37 +131,47 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
   // -------- stress evaluators on plane pointers --------
   // U0/Up: u tiles of planes i and i+1 (Um: i-1); M0/Mp material tiles of i, i+1.
   // d = offset of the evaluated position from the own one inside a tile.
-  // T1..T3 at (i, j+dj, k+dk): the caller supplies validity and spacings.
-  auto T123 = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, bool kzero, R sa, R sb, R sd,
-                  R& T1, R& T2, R& T3, bool want3) {
+  // The traction-free row (k = 0) differs from the interior only in the
+  // spacings and material index it uses: its "uz - 0" is the interior
+  // difference against the zero padding at k = -1.  So each stress is one
+  // evaluation on selected operands, never two evaluations and a select.
+  auto T123 = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, R sa, R sb, R sd, R& T1, R& T2,
+                  R& T3) {
     const R* c = tab + 16 * M0[Lm + dm];
     const R d1 = S::sub(U0[XO + Lu + du], Um[XO + Lu + du]);
     const R d2 = S::sub(U0[YO + Lu + du], U0[YO + Lu + du - KW]);
-    const R d3 = kzero ? U0[ZO + Lu + du] : S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
+    const R d3 = S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
     T1 = S::tn1(c, d1, d2, d3, sa, sb, sd);
     T2 = S::tn1(c + 3, d1, d2, d3, sa, sb, sd);
-    T3 = want3 ? S::tn1(c + 6, d1, d2, d3, sa, sb, sd) : R(0);
+    T3 = S::tn1(c + 6, d1, d2, d3, sa, sb, sd);
+  };
+  auto T1one = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, int which, R sa, R sb, R sd) {
+    const R* c = tab + 16 * M0[Lm + dm] + 3 * which;
+    const R d1 = S::sub(U0[XO + Lu + du], Um[XO + Lu + du]);
+    const R d2 = S::sub(U0[YO + Lu + du], U0[YO + Lu + du - KW]);
+    const R d3 = S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
+    return S::tn1(c, d1, d2, d3, sa, sb, sd);
   };
   // T4 (base_solver.py:353-358, 420-423)
   auto T4f = [&](const R* U0, const uint8_t* M0, int du, int dm, bool kzero, R fz, R fy) {
     const R c = tab[16 * M0[Lm + dm + MKW + (kzero ? 0 : 1)] + 9];
     const R d1 = S::sub(U0[YO + Lu + du + 1], U0[YO + Lu + du]);
     const R d2 = S::sub(U0[ZO + Lu + du + KW], U0[ZO + Lu + du]);
-    return kzero ? S::ts(c, d1, a.sp.fdy0, d2, a.sp.fdz0) : S::ts(c, d1, fz, d2, fy);
+    return S::ts(c, d1, kzero ? a.sp.fdy0 : fz, d2, kzero ? a.sp.fdz0 : fy);
   };
   // T5 (base_solver.py:360-365, 425-428)
   auto T5f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fz, R fx) {
     const R c = tab[16 * Mp[Lm + dm + (kzero ? 0 : 1)] + 10];
     const R d1 = S::sub(U0[XO + Lu + du + 1], U0[XO + Lu + du]);
     const R d2 = S::sub(Up[ZO + Lu + du], U0[ZO + Lu + du]);
-    return kzero ? S::ts(c, d1, a.sp.fdx0, d2, a.sp.fdz0) : S::ts(c, d1, fz, d2, fx);
+    return S::ts(c, d1, kzero ? a.sp.fdx0 : fz, d2, kzero ? a.sp.fdz0 : fx);
   };
   // T6 (base_solver.py:367-372, 430-433)
   auto T6f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fy, R fx) {
     const R c = tab[16 * Mp[Lm + dm + MKW] + 11];
     const R d1 = S::sub(U0[XO + Lu + du + KW], U0[XO + Lu + du]);
     const R d2 = S::sub(Up[YO + Lu + du], U0[YO + Lu + du]);
-    return kzero ? S::ts(c, d1, a.sp.fdx0, d2, a.sp.fdz0) : S::ts(c, d1, fy, d2, fx);
+    return S::ts(c, d1, kzero ? a.sp.fdx0 : fy, d2, kzero ? a.sp.fdz0 : fx);
   };
 
   // prologue stresses: own T5, T6 at plane ib-1
@@ -166,7 +186,7 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
     t5m = (i_s && j_n && k_in) ? T5f(U0, Up, Mp, 0, 0, kz, fdz_k, fx) : R(0);
     t6m = (i_s && j_s && k_in) ? T6f(U0, Up, Mp, 0, 0, kz, fdy_j, fx) : R(0);
   }
-  R t1m = 0, uxm = 0;
+  R t1m = 0, uxm = 0, uxm_up = 0;
 
   // pointwise state prefetch, one plane ahead: ux at plane i-1, uy/uz at plane i
   // (V0 points only: u_new there depends on u_old / v / c of the same point)
@@ -201,7 +221,8 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
     // own stresses at plane i
     R t1c, t2c, t3c;
     if (i_n && j_n && k_in) {
-      T123(Um, U0, M0, 0, 0, kz, kz ? a.sp.sdx0 : sdx_im, t123_b, t123_d, t1c, t2c, t3c, !kz);
+      T123(Um, U0, M0, 0, 0, kz ? a.sp.sdx0 : sdx_im, t123_b, t123_d, t1c, t2c, t3c);
+      if (kz) t3c = R(0);  // T3[1:-1,1:-1,0] = 0 (base_solver.py:418)
     } else {
       t1c = t2c = t3c = R(0);
     }
@@ -225,11 +246,8 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
         R v = R(0);
         if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2) {
           const bool z0 = kk == 0;
-          R x1, x2, x3;
-          T123(Um, U0, M0, du0 + TJ * KW + qq, dm0 + TJ * MKW + qq, z0, z0 ? a.sp.sdx0 : sdx_im,
-               z0 ? a.sp.sdy0 : __ldg(a.sp.sdy + jj - 1), z0 ? a.sp.sdz0 : __ldg(a.sp.sdz + kk - 1), x1, x2, x3,
-               false);
-          v = x2;
+          v = T1one(Um, U0, M0, du0 + TJ * KW + qq, dm0 + TJ * MKW + qq, 1, z0 ? a.sp.sdx0 : sdx_im,
+                    z0 ? a.sp.sdy0 : __ldg(a.sp.sdy + jj - 1), z0 ? a.sp.sdz0 : __ldg(a.sp.sdz + kk - 1));
         }
         sT2[(TJ + 1) * W + qq + 1] = v;
       } else if (qq < 2 * TK) {  // T6 at (j0-1, k0+q)
@@ -251,12 +269,9 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
         if (which == 0) {  // T3 at (j0+jl, k0+TK)
           const int kk = k0 + TK;
           R v = R(0);
-          if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2) {
-            R x1, x2, x3;  // kk >= 32: never the z = 0 row
-            T123(Um, U0, M0, du0 + jl * KW + TK, dm0 + jl * MKW + TK, false, sdx_im, __ldg(a.sp.sdy + jj - 1),
-                 __ldg(a.sp.sdz + kk - 1), x1, x2, x3, true);
-            v = x3;
-          }
+          if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2)  // kk >= 32: never the z = 0 row
+            v = T1one(Um, U0, M0, du0 + jl * KW + TK, dm0 + jl * MKW + TK, 2, sdx_im, __ldg(a.sp.sdy + jj - 1),
+                      __ldg(a.sp.sdz + kk - 1));
           sT3[(jl + 1) * W + TK + 1] = v;
         } else if (which == 1) {  // T4 at (j0+jl, k0-1)
           const int kk = k0 - 1;
@@ -275,6 +290,7 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
       }
     }
     const R uxc = U0[XO + Lu], uyc = U0[YO + Lu], uzc = U0[ZO + Lu];
+    const R uxc_up = U0[XO + Lu + 1];  // ux(i, j, k+1): z = N face input of the next plane's ux
     __syncthreads();
     // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
     if (tid == 0 && i - 1 + NSLOT <= plast) {
@@ -285,66 +301,67 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
       if (i < ie) {
         // uy_new(i, j, k)   (base_solver.py:449-455, 503-509)
         if (!face_y) {
+          R val;
           if (i_n) {
+            // at k = 0 the T4(k-1) halo entry is 0, so T4 - 0 is the z = 0 row's "T4 - 0"
             const R* row = tab + 16 * M0[Lm + MKW];
-            const R dv = kz ? S::div3(S::sub(t6c, t6m), a.sp.sdx0, S::sub(sT2[L + W], t2c), a.sp.fdy0, t4c, a.sp.sdz0)
-                            : S::div3(S::sub(t6c, t6m), sdx_im, S::sub(sT2[L + W], t2c), fdy_j,
-                                      S::sub(t4c, sT4[L - 1]), sdz_m);
+            const R dv = S::div3(S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
+                                 S::sub(t4c, sT4[L - 1]), uy_c);
             R vn, cn;
-            const R un = update_value<S>(uyc, pwy, dv, row, vn, cn);
-            store_point<S>(r, 1, off_i, un, vn, cn);
+            val = update_value<S>(uyc, pwy, dv, row, vn, cn);
+            store_point<S>(r, 1, off_i, val, vn, cn);
           } else {
-            store_stale<S>(r, 1, off_i);
+            val = store_stale<S>(r, 1, off_i);
           }
+          if (zface_xy)  // uy on z = N from its inner neighbour (base_solver.py:553)
+            store_point<S>(r, 1, off_i + 1, rigid ? R(0) : S::abc(a.abc[6], val, U0[YO + Lu + 1], uyc), R(0), R(0));
         }
         // uz_new(i, j, k)   (base_solver.py:457-463, 511-516)
         if (!face_z) {
           R val;
           if (i_n && j_n) {
-            R dv;
-            const R* row;
-            if (kz) {
-              row = tab + 16 * M0[Lm];  // density at z index 0 (base_solver.py:513)
-              dv = a.surface_mode == 0
-                       ? S::div_surf_ref(S::sub(t5c, t5m), a.sp.sdx0, S::sub(t4c, sT4[L - W]), a.sp.sdy0, sT3[L + 1])
-                       : S::div3(S::sub(t5c, t5m), a.sp.sdx0, S::sub(t4c, sT4[L - W]), a.sp.sdy0, sT3[L + 1],
-                                 a.sp.fdz0);
-            } else {
-              row = tab + 16 * M0[Lm + 1];
-              dv = S::div3(S::sub(t5c, t5m), sdx_im, S::sub(t4c, sT4[L - W]), sdy_m, S::sub(sT3[L + 1], t3c), fdz_k);
-            }
+            // z = 0 row: density at z index 0 (base_solver.py:513); T3(k) = 0 there,
+            // and the reference precedence (:516) adds T3[..,1] with factor 1
+            const R* row = tab + 16 * M0[Lm + (kz ? 0 : 1)];
+            const R dv = S::div3(S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
+                                 S::sub(sT3[L + 1], t3c), uz_c);
             R vn, cn;
             val = update_value<S>(uzc, pwz, dv, row, vn, cn);
             store_point<S>(r, 2, off_i, val, vn, cn);
           } else {
-            store_stale<S>(r, 2, off_i);
-            val = __ldg(r.cur(2) + off_i);
+            val = store_stale<S>(r, 2, off_i);
           }
           if (kz) record(a, tt, i, j, val);
+          if (zface_z)  // uz on z = N from its inner neighbour (base_solver.py:554)
+            store_point<S>(r, 2, off_i + 1, rigid ? R(0) : S::abc(a.abc[7], val, U0[ZO + Lu + 1], uzc), R(0), R(0));
         }
       }
       if (i > ib && !face_x && i - 1 != nx - 2) {
         // ux_new(i-1, j, k)   (base_solver.py:441-447, 495-501)
         const long long off = off_i - g.sx;
+        R val;
         if (j_n) {
           const int pm = p ^ 1;
           const R* row = tab + 16 * M0[Lm];  // P[(i-1)+1, j, k]
-          const R dv = kz ? S::div3(S::sub(t1c, t1m), a.sp.fdx0, S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]),
-                                    a.sp.sdy0, sT5[pm * PL + L], a.sp.sdz0)
-                          : S::div3(S::sub(t1c, t1m), fdx_im, S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]), sdy_m,
-                                    S::sub(sT5[pm * PL + L], sT5[pm * PL + L - 1]), sdz_m);
+          // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
+          const R dv = S::div3(S::sub(t1c, t1m), kz ? a.sp.fdx0 : fdx_im,
+                               S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]), ux_b,
+                               S::sub(sT5[pm * PL + L], sT5[pm * PL + L - 1]), ux_c);
           R vn, cn;
-          const R un = update_value<S>(uxm, pwx, dv, row, vn, cn);
-          store_point<S>(r, 0, off, un, vn, cn);
+          val = update_value<S>(uxm, pwx, dv, row, vn, cn);
+          store_point<S>(r, 0, off, val, vn, cn);
         } else {
-          store_stale<S>(r, 0, off);
+          val = store_stale<S>(r, 0, off);
         }
+        if (zface_xy)  // ux on z = N from its inner neighbour (base_solver.py:552)
+          store_point<S>(r, 0, off + 1, rigid ? R(0) : S::abc(a.abc[6], val, uxm_up, uxm), R(0), R(0));
       }
     }
     t1m = t1c;
     t5m = t5c;
     t6m = t6c;
     uxm = uxc;
+    uxm_up = uxc_up;
     pwx = nx_;
     pwy = ny_;
     pwz = nz_;
