@@ -187,6 +187,29 @@ typedef struct phono_energy_dense {
 
 int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *stream);
 
+/* Batches: many simulations stepped together.  Every time step is one
+ * persistent tile launch (CTAs pull (instance, tile) work items until none
+ * are left) and one face launch for all active instances, replayed from a
+ * captured CUDA graph.  The reference runs one simulation per solver object
+ * (base_solver.py:245-266) and has no counterpart; the per-instance
+ * arithmetic is that of phono_step, bit for bit.  Instances are handles made
+ * by phono_create with the batch's precision and tile_j and ny >= 4; while a
+ * handle is in a batch, step it only through the batch and call
+ * phono_batch_sync before reading it. */
+typedef struct phono_batch phono_batch;
+
+int phono_batch_create(int capacity, int precision, int tile_j, phono_batch **out);
+/* Attach h for nsteps more steps; returns the slot (>= 0) or an error code. */
+int phono_batch_add(phono_batch *b, phono_handle *h, int nsteps);
+int phono_batch_remove(phono_batch *b, int slot);
+/* Steps an instance still has to take (0 when done). */
+int phono_batch_remaining(const phono_batch *b, int slot);
+/* Advance every active instance by up to nsteps (each stops at its budget). */
+int phono_batch_step(phono_batch *b, int nsteps);
+int phono_batch_sync(phono_batch *b);
+int phono_batch_last_step_ms(phono_batch *b, float *ms);
+void phono_batch_destroy(phono_batch *b);
+
 /* Device time of the last phono_step call in milliseconds (CUDA events). */
 int phono_last_step_ms(phono_handle *h, float *ms);
 

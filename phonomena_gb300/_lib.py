@@ -25,7 +25,9 @@ FIELDS = {"ux": 0, "uy": 1, "uz": 2, "ux_old": 3, "uy_old": 4, "uz_old": 5,
 EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done", "phono_reset",
            "phono_set_materials", "phono_stream", "phono_sync",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
-           "phono_energy_static",
+           "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
+           "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
+           "phono_batch_destroy",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
 
@@ -91,6 +93,14 @@ def load(path: Path | None = None):
         "phono_elem_size": (ci, [vp]),
         "phono_energy": (ci, [vp, vp]),
         "phono_energy_static": (ci, [ctypes.POINTER(PhonoEnergyDense), vp, vp]),
+        "phono_batch_create": (ci, [ci, ci, ci, ctypes.POINTER(vp)]),
+        "phono_batch_add": (ci, [vp, vp, ci]),
+        "phono_batch_remove": (ci, [vp, ci]),
+        "phono_batch_remaining": (ci, [vp, ci]),
+        "phono_batch_step": (ci, [vp, ci]),
+        "phono_batch_sync": (ci, [vp]),
+        "phono_batch_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
+        "phono_batch_destroy": (None, [vp]),
         "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_destroy": (None, [vp]),
         "phono_last_error": (ctypes.c_char_p, []),

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <algorithm>
 
 #include "../../include/phono.h"
 #include <cudaTypedefs.h>
@@ -17,6 +18,9 @@ cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int n_face_blocks
 cudaError_t configure_step_f64v(int tj);
 cudaError_t launch_step_f64v(const StepArgs<double>& a, int tj, int n_face_blocks, cudaStream_t st);
 cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st);
+cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st);
+cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, int n, cudaStream_t st);
+cudaError_t batch_configure_any(int precision, int tj, int* blocks_per_sm);
 
 __global__ void advance_step_kernel(int* p, int n) { *p += n; }
 }  // namespace phono
@@ -225,6 +229,7 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.n_tile_blocks = h->n_tile;
   a.faces = h->faces;
   a.err = h->err;
+  a.step_end = 0x7fffffff;
   return a;
 }
 
@@ -674,5 +679,287 @@ int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table
 void* phono_stream(phono_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 void phono_destroy(phono_handle* h) { release(h); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+struct phono_batch {
+  int cap = 0, precision = 0, tj = 8;
+  size_t inst_size = 0;  // sizeof(StepArgs<R>)
+  std::vector<void*> allocs;
+  char* d_inst = nullptr;
+  int2* d_items = nullptr;
+  int item_cap = 0;
+  int* d_counts = nullptr;  // items, face blocks, face entries, active instances
+  unsigned* d_ticket = nullptr;
+  int* d_face_prefix = nullptr;
+  int* d_face_inst = nullptr;
+  int* d_active = nullptr;
+  std::vector<phono_handle*> slot;
+  std::vector<int> remaining;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false, dirty = true;
+  int grid_tiles = 0, grid_faces = 0;
+};
+
+static void batch_release(phono_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+static int balloc(phono_batch* b, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(PHONO_ERR_NOMEM, std::string("cudaMalloc ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+  }
+  b->allocs.push_back(*p);
+  return PHONO_OK;
+}
+
+// BatchArgs over the batch's device tables (same layout for float and double)
+static BatchArgs<float> batch_args(const phono_batch* b, int step_off) {
+  BatchArgs<float> ba{};
+  ba.inst = reinterpret_cast<const StepArgs<float>*>(b->d_inst);
+  ba.items = b->d_items;
+  ba.counts = b->d_counts;
+  ba.ticket = b->d_ticket;
+  ba.face_prefix = b->d_face_prefix;
+  ba.face_inst = b->d_face_inst;
+  ba.active = b->d_active;
+  ba.step_off = step_off;
+  return ba;
+}
+static_assert(sizeof(BatchArgs<float>) == sizeof(BatchArgs<double>), "batch argument layouts differ");
+
+// work items (costliest instances first), face-block prefix, active list
+static int batch_rebuild(phono_batch* b) {
+  std::vector<int> act;
+  for (int s = 0; s < b->cap; s++)
+    if (b->slot[s] && b->remaining[s] > 0) act.push_back(s);
+  std::sort(act.begin(), act.end(), [&](int x, int y) {
+    long long cx = (long long)b->slot[x]->n_tile, cy = (long long)b->slot[y]->n_tile;
+    return cx != cy ? cx > cy : x < y;
+  });
+  std::vector<int2> items;
+  std::vector<int> prefix, finst;
+  int fb = 0;
+  for (int s : act) {
+    const phono_handle* h = b->slot[s];
+    for (int t = 0; t < h->n_tile; t++) items.push_back(make_int2(s, t));
+    prefix.push_back(fb);
+    finst.push_back(s);
+    fb += (h->faces.off[12] + 255) / 256;
+  }
+  prefix.push_back(fb);
+  if ((int)items.size() > b->item_cap) {
+    int cap = std::max<int>((int)items.size(), 2 * b->item_cap);
+    void* p = nullptr;
+    int rc = balloc(b, &p, (size_t)cap * sizeof(int2));
+    if (rc) return rc;
+    b->d_items = (int2*)p;
+    b->item_cap = cap;
+    if (b->graph) {  // the captured launches hold the old pointer
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  int counts[4] = {(int)items.size(), fb, (int)finst.size(), (int)act.size()};
+  if (!items.empty())
+    CK(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->d_face_prefix, prefix.data(), prefix.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  if (!finst.empty()) {
+    CK(cudaMemcpyAsync(b->d_face_inst, finst.data(), finst.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_active, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
+  CK(cudaMemcpyAsync(b->d_counts, counts, sizeof counts, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned), b->stream));
+  CK(cudaStreamSynchronize(b->stream));  // host vectors go out of scope
+  b->dirty = false;
+  return PHONO_OK;
+}
+
+static cudaError_t batch_launch_steps(phono_batch* b, int first_off, int n) {
+  for (int s = 0; s < n; s++) {
+    BatchArgs<float> ba = batch_args(b, first_off + s);
+    cudaError_t e = batch_step_any(b->precision, &ba, b->tj, b->grid_tiles, b->grid_faces, b->stream);
+    if (e != cudaSuccess) return e;
+  }
+  BatchArgs<float> ba = batch_args(b, 0);
+  return batch_advance_any(b->precision, &ba, b->cap, n, b->stream);
+}
+
+extern "C" {
+
+int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** out) {
+  if (!out) return fail(PHONO_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (capacity < 1 || capacity > (1 << 20)) return fail(PHONO_ERR_ARG, "capacity must be in 1..2^20");
+  if (precision != PHONO_F64 && precision != PHONO_F32K && precision != PHONO_F64V)
+    return fail(PHONO_ERR_ARG, "unknown precision");
+  if (tile_j == 0) tile_j = 8;
+  if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 4, 8 or 16");
+  phono_batch* b = new phono_batch();
+  b->cap = capacity;
+  b->precision = precision;
+  b->tj = tile_j;
+  b->inst_size = precision == PHONO_F32K ? sizeof(StepArgs<float>) : sizeof(StepArgs<double>);
+  b->slot.assign(capacity, nullptr);
+  b->remaining.assign(capacity, 0);
+#define BTRY(x)              \
+  do {                       \
+    int r_ = (x);            \
+    if (r_) {                \
+      std::string m_ = g_err; \
+      batch_release(b);      \
+      g_err = m_;            \
+      return r_;             \
+    }                        \
+  } while (0)
+#define BTRYC(x)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (x);                                                             \
+    if (e_ != cudaSuccess) {                                                          \
+      batch_release(b);                                                               \
+      return fail(PHONO_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));   \
+    }                                                                                 \
+  } while (0)
+  BTRYC(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BTRYC(cudaEventCreate(&b->ev0));
+  BTRYC(cudaEventCreate(&b->ev1));
+  BTRY(balloc(b, (void**)&b->d_inst, b->inst_size * capacity));
+  BTRY(balloc(b, (void**)&b->d_counts, sizeof(int) * 4));
+  BTRY(balloc(b, (void**)&b->d_ticket, sizeof(unsigned)));
+  BTRY(balloc(b, (void**)&b->d_face_prefix, sizeof(int) * (capacity + 1)));
+  BTRY(balloc(b, (void**)&b->d_face_inst, sizeof(int) * capacity));
+  BTRY(balloc(b, (void**)&b->d_active, sizeof(int) * capacity));
+  BTRYC(cudaMemset(b->d_counts, 0, sizeof(int) * 4));
+  BTRYC(cudaMemset(b->d_ticket, 0, sizeof(unsigned)));
+  int bps = 0, dev = 0, nsm = 0;
+  BTRYC(batch_configure_any(precision, tile_j, &bps));
+  BTRYC(cudaGetDevice(&dev));
+  BTRYC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  b->grid_tiles = std::max(1, bps) * nsm;
+  b->grid_faces = 8 * nsm;
+#undef BTRY
+#undef BTRYC
+  *out = b;
+  return PHONO_OK;
+}
+
+int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
+  if (!b || !h) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->d.precision != b->precision) return fail(PHONO_ERR_ARG, "handle precision differs from the batch");
+  if (h->tj != b->tj) return fail(PHONO_ERR_ARG, "handle tile_j differs from the batch");
+  if (!h->separate_faces) return fail(PHONO_ERR_ARG, "batched instances need ny >= 4");
+  if (nsteps < 0 || h->steps_done + nsteps > h->nsrc)
+    return fail(PHONO_ERR_STATE, "not enough source samples for the requested steps");
+  int s = -1;
+  for (int q = 0; q < b->cap; q++) {
+    if (b->slot[q] == h) return fail(PHONO_ERR_ARG, "handle already in the batch");
+    if (s < 0 && !b->slot[q]) s = q;
+  }
+  if (s < 0) return fail(PHONO_ERR_NOMEM, "batch is full");
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->precision == PHONO_F32K) {
+    StepArgs<float> a = make_args<float>(h, 0);
+    a.step_end = h->steps_done + nsteps;
+    CK(cudaMemcpy(b->d_inst + (size_t)s * b->inst_size, &a, sizeof a, cudaMemcpyHostToDevice));
+  } else {
+    StepArgs<double> a = make_args<double>(h, 0);
+    a.step_end = h->steps_done + nsteps;
+    CK(cudaMemcpy(b->d_inst + (size_t)s * b->inst_size, &a, sizeof a, cudaMemcpyHostToDevice));
+  }
+  b->slot[s] = h;
+  b->remaining[s] = nsteps;
+  b->dirty = true;
+  return s;
+}
+
+int phono_batch_remove(phono_batch* b, int s) {
+  if (!b || s < 0 || s >= b->cap || !b->slot[s]) return fail(PHONO_ERR_ARG, "no instance in that slot");
+  CK(cudaStreamSynchronize(b->stream));
+  b->slot[s] = nullptr;
+  b->remaining[s] = 0;
+  b->dirty = true;
+  return PHONO_OK;
+}
+
+int phono_batch_remaining(const phono_batch* b, int s) {
+  if (!b || s < 0 || s >= b->cap || !b->slot[s]) return fail(PHONO_ERR_ARG, "no instance in that slot");
+  return b->remaining[s];
+}
+
+int phono_batch_step(phono_batch* b, int nsteps) {
+  if (!b) return fail(PHONO_ERR_ARG, "batch is NULL");
+  if (nsteps < 0) return fail(PHONO_ERR_ARG, "nsteps < 0");
+  if (nsteps == 0) return PHONO_OK;
+  if (b->dirty) {
+    for (int s = 0; s < b->cap; s++)
+      if (b->slot[s]) CK(cudaStreamSynchronize(b->slot[s]->stream));
+    int rc = batch_rebuild(b);
+    if (rc) return rc;
+  }
+  if (!b->graph && nsteps >= kGraphSteps) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = batch_launch_steps(b, 0, kGraphSteps);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail(PHONO_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(b->ev0, b->stream));
+  const int full = nsteps / kGraphSteps, rem = nsteps % kGraphSteps;
+  for (int q = 0; q < full; q++) CK(cudaGraphLaunch(b->graph, b->stream));
+  if (rem) CK(batch_launch_steps(b, 0, rem));
+  CK(cudaEventRecord(b->ev1, b->stream));
+  b->timed = true;
+  for (int s = 0; s < b->cap; s++) {
+    if (!b->slot[s] || b->remaining[s] <= 0) continue;
+    const int adv = std::min(nsteps, b->remaining[s]);
+    b->remaining[s] -= adv;
+    b->slot[s]->steps_done += adv;
+    if (b->remaining[s] == 0) b->dirty = true;
+  }
+  return PHONO_OK;
+}
+
+int phono_batch_sync(phono_batch* b) {
+  if (!b) return fail(PHONO_ERR_ARG, "batch is NULL");
+  CK(cudaStreamSynchronize(b->stream));
+  for (int s = 0; s < b->cap; s++) {
+    if (!b->slot[s]) continue;
+    int err = 0;
+    CK(cudaMemcpy(&err, b->slot[s]->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(PHONO_ERR_NUMERIC, "instance " + std::to_string(s) + ": non-finite surface value or stalled pipeline");
+  }
+  return PHONO_OK;
+}
+
+int phono_batch_last_step_ms(phono_batch* b, float* ms) {
+  if (!b || !ms) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (!b->timed) return fail(PHONO_ERR_STATE, "no step timed yet");
+  CK(cudaEventSynchronize(b->ev1));
+  CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+  return PHONO_OK;
+}
+
+void phono_batch_destroy(phono_batch* b) { batch_release(b); }
 
 }  // extern "C"

@@ -99,6 +99,21 @@ struct StepArgs {
   int n_tile_blocks;
   FaceTable faces;
   int* __restrict__ err;  // device error flags: 1 non-finite surface value, 2 pipeline wait timed out
+  int step_end;           // global steps >= step_end are skipped (a batched instance's budget)
+};
+
+// Batched launch: many instances (each a StepArgs in device memory) share one
+// persistent tile launch and one face launch per step.
+template <class R>
+struct BatchArgs {
+  const StepArgs<R>* inst;  // [capacity] per-instance arguments
+  const int2* items;        // (instance, tile) work items, costliest first
+  const int* counts;        // [0] work items, [1] face blocks, [2] entries of face_prefix
+  unsigned* ticket;         // work-item counter; returns to 0 after every launch
+  const int* face_prefix;   // first face block of each listed instance (+ total)
+  const int* face_inst;     // instance of each listed entry
+  const int* active;        // [counts[3]] active instances (step-counter update)
+  int step_off;             // offset of this launch inside a captured chunk of steps
 };
 
 // arguments of the energy reduction (energy.cu)

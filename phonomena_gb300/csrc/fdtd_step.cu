@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ 
   }
 
   // ---------------- tile blocks ----------------
-  tile_block<S, TJ>(a, base, r, s, tt, tid);
+  tile_block<S, TJ>(a, base, r, s, tt, tid, blockIdx.x, &a.tm_u, &a.tm_mat);
 }
 
 // ---------------------------------------------------------------------------
@@ -658,6 +658,124 @@ cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int separate_f
     case 16: return launch_tj<S, 16>(a, separate_faces, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// ---------------------------------------------------------------------------
+// batched instances: persistent tile kernel + face kernel + counter update
+// ---------------------------------------------------------------------------
+template <class S, int TJ>
+__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : (TJ < 16 ? 16 / TJ : 1)))
+    batch_step_kernel(const __grid_constant__ BatchArgs<typename S::R> ba) {
+  using R = typename S::R;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  __shared__ StepArgs<R> sa;  // the current item's instance arguments
+  __shared__ int item;
+  const int tid = threadIdx.y * TK + threadIdx.x;
+  const int n_items = __ldg(ba.counts);
+  for (;;) {
+    // each block takes items until one past the end; the counter wraps to 0
+    // after the last of the n_items + gridDim.x requests
+    if (tid == 0) item = (int)atomicInc(ba.ticket, (unsigned)(n_items + gridDim.x - 1));
+    __syncthreads();
+    const int it = item;
+    if (it >= n_items) break;
+    const int2 w = ba.items[it];
+    const int4* src4 = reinterpret_cast<const int4*>(ba.inst + w.x);
+    int4* dst4 = reinterpret_cast<int4*>(&sa);
+    for (int q = tid; q < (int)(sizeof(StepArgs<R>) / 16); q += TK * TJ) dst4[q] = src4[q];
+    __syncthreads();
+    const int tt = *sa.step_base + ba.step_off;
+    if (tt < sa.step_end) {
+      const Roles<R> r = roles<S>(sa, tt);
+      tile_block<S, TJ>(sa, base, r, (R)__ldg(sa.src + tt), tt, tid, w.y, &ba.inst[w.x].tm_u, &ba.inst[w.x].tm_mat);
+    }
+    __syncthreads();  // sa and item are rewritten by the next iteration
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) batch_face_kernel(const __grid_constant__ BatchArgs<typename S::R> ba) {
+  using R = typename S::R;
+  const int n_fb = __ldg(ba.counts + 1), n_ent = __ldg(ba.counts + 2);
+  for (int fb = blockIdx.x; fb < n_fb; fb += gridDim.x) {
+    int lo = 0, hi = n_ent - 1;  // last entry whose first block <= fb
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(ba.face_prefix + mid) <= fb) lo = mid;
+      else hi = mid - 1;
+    }
+    const StepArgs<R>& a = ba.inst[__ldg(ba.face_inst + lo)];
+    const int tt = *a.step_base + ba.step_off;
+    if (tt >= a.step_end) continue;
+    const Roles<R> r = roles<S>(a, tt);
+    face_point<S>(a, r, (R)__ldg(a.src + tt), tt, (fb - __ldg(ba.face_prefix + lo)) * 256 + threadIdx.x, true);
+  }
+}
+
+// advance the step counter of every active instance by n, stopping at its budget
+template <class R>
+__global__ void batch_advance_kernel(const __grid_constant__ BatchArgs<R> ba, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= __ldg(ba.counts + 3)) return;
+  const StepArgs<R>& a = ba.inst[__ldg(ba.active + q)];
+  int* c = const_cast<int*>(a.step_base);
+  *c = min(*c + n, a.step_end);
+}
+
+template <class S, int TJ>
+static cudaError_t batch_launch_tj(const BatchArgs<typename S::R>& ba, int grid_tiles, int grid_faces,
+                                   cudaStream_t st) {
+  batch_step_kernel<S, TJ><<<grid_tiles, dim3(TK, TJ), SmemPlan<typename S::R, TJ>::total, st>>>(ba);
+  batch_face_kernel<S><<<grid_faces, 256, 0, st>>>(ba);
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t batch_step(const BatchArgs<typename S::R>& ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st) {
+  switch (tj) {
+    case 4: return batch_launch_tj<S, 4>(ba, grid_tiles, grid_faces, st);
+    case 8: return batch_launch_tj<S, 8>(ba, grid_tiles, grid_faces, st);
+    case 16: return batch_launch_tj<S, 16>(ba, grid_tiles, grid_faces, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <class S, int TJ>
+static cudaError_t batch_configure_tj(int* blocks_per_sm) {
+  const int smem = (int)SmemPlan<typename S::R, TJ>::total;
+  cudaError_t e = cudaFuncSetAttribute(batch_step_kernel<S, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_step_kernel<S, TJ>, TK * TJ, smem);
+}
+
+template <class S>
+cudaError_t batch_configure(int tj, int* blocks_per_sm) {
+  switch (tj) {
+    case 4: return batch_configure_tj<S, 4>(blocks_per_sm);
+    case 8: return batch_configure_tj<S, 8>(blocks_per_sm);
+    case 16: return batch_configure_tj<S, 16>(blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st) {
+  if (precision == 0) return batch_step<F64>(*(const BatchArgs<double>*)ba, tj, grid_tiles, grid_faces, st);
+  if (precision == 2) return batch_step<F64V>(*(const BatchArgs<double>*)ba, tj, grid_tiles, grid_faces, st);
+  return batch_step<F32K>(*(const BatchArgs<float>*)ba, tj, grid_tiles, grid_faces, st);
+}
+
+cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, int n, cudaStream_t st) {
+  const int blocks = (n_active_cap + 255) / 256;
+  if (precision == 1) batch_advance_kernel<float><<<blocks, 256, 0, st>>>(*(const BatchArgs<float>*)ba, n);
+  else batch_advance_kernel<double><<<blocks, 256, 0, st>>>(*(const BatchArgs<double>*)ba, n);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_configure_any(int precision, int tj, int* blocks_per_sm) {
+  if (precision == 0) return batch_configure<F64>(tj, blocks_per_sm);
+  if (precision == 2) return batch_configure<F64V>(tj, blocks_per_sm);
+  return batch_configure<F32K>(tj, blocks_per_sm);
 }
 
 // non-template entry points for the C ABI translation unit

@@ -14,9 +14,10 @@
 #pragma once
 
 template <class S, int TJ>
-__device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, unsigned char* base,
+__device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, unsigned char* base,
                                            const Roles<typename S::R>& r, const typename S::R s, const int tt,
-                                           const int tid) {
+                                           const int tid, const int b, const CUtensorMap* tm_u,
+                                           const CUtensorMap* tm_mat) {
   using R = typename S::R;
   using P = SmemPlan<R, TJ>;
   using TF = TileFetch<R, TJ>;
@@ -37,7 +38,6 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
 
   const Geo& g = a.g;
   const int nx = g.nx, ny = g.ny, nz = g.nz;
-  const int b = blockIdx.x;
   const int kt = b % a.ntk;
   const int rest = b / a.ntk;
   const int jt = rest % a.ntj;
@@ -90,8 +90,8 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
     const int q = p - ibase, sl = q & (NSLOT - 1);
     mbar_expect_tx(&bars[sl], P::tx_bytes);
     // padded coordinates: k + KOFF, j + 1, i + 1; the tiles start at k0-KB, j0-1
-    tma_load_4d(uring + sl * SU, &a.tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
-    tma_load_3d(mring + sl * SM, &a.tm_mat, k0, j0, p + 1, &bars[sl]);
+    tma_load_4d(uring + sl * SU, tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
+    tma_load_3d(mring + sl * SM, tm_mat, k0, j0, p + 1, &bars[sl]);
   };
   bool ok = true;
   auto wait_plane = [&](int p) {
@@ -375,7 +375,13 @@ __device__ __forceinline__ void tile_block(const StepArgs<typename S::R>& a, uns
         mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1);
       }
     }
-    __syncthreads();
   }
+  // every issued plane has been waited for; the barriers may be set up
+  // again by the next tile of a persistent block
+  __syncthreads();
+  if (tid == 0)
+    for (int q = 0; q < NSLOT; q++) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[q])) : "memory");
+  __syncthreads();
+  return ok;
 }
 

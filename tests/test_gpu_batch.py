@@ -1,0 +1,106 @@
+"""Batched instances (one persistent launch for many crystals) against the
+same instances stepped alone: every field and surface record must be
+bit-identical, whatever the mix, the budgets and the join/leave order."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(40, 36, 20), (33, 48, 17), (64, 40, 30), (20, 20, 12), (50, 45, 33)]
+BUDGETS = [60, 37, 60, 13, 48]
+
+
+def _sim(cells, seed, precision, steps, tile_j=8, x_segment=16):
+    from phonomena_gb300 import crystal
+    from phonomena_gb300.device import DeviceSimulation
+
+    spec = crystal.CrystalSpec(cells=cells, lattice=8, radius=(0.2, 0.4), tungsten_frac=0.25, seed=seed,
+                               freq=30e6 + 5e6 * seed, steps=steps)
+    g, m = crystal.build(spec)
+    sim = DeviceSimulation(g.spacing(), m.ids, m.table, m.dt, precision=precision, surface_mode="corrected",
+                           max_steps=steps, record_every=5, tile_j=tile_j, x_segment=x_segment)
+    sim.set_source(crystal.sin_source(spec.freq, m.dt, steps))
+    return sim
+
+
+def _state(sim):
+    sim.sync()
+    return [sim.download(k) for k in ("ux", "uy", "uz")], sim.read_surface()
+
+
+@pytest.mark.parametrize("precision", ["f32k", "f64", "f64v"])
+def test_batch_bit_identical_to_alone(gpu_lib, precision):
+    from phonomena_gb300.batch import Batch
+
+    alone = []
+    for q, (cells, n) in enumerate(zip(SHAPES, BUDGETS)):
+        s = _sim(cells, q, precision, 60)
+        s.step(n)
+        alone.append(_state(s))
+        s.close()
+    sims = [_sim(cells, q, precision, 60) for q, cells in enumerate(SHAPES)]
+    with Batch(8, precision=precision, tile_j=8) as b:
+        slots = [b.add(s, n) for s, n in zip(sims, BUDGETS)]
+        b.step(25)
+        b.step(1)
+        b.step(40)  # more than any budget left: every instance stops at its own
+        b.sync()
+        for s, slot, n in zip(sims, slots, BUDGETS):
+            assert b.remaining(slot) == 0
+            assert s.steps_done == n
+    for q, s in enumerate(sims):
+        got = _state(s)
+        for a, e in zip(got[0], alone[q][0]):
+            assert np.array_equal(a, e), f"instance {q}: field differs from the alone run"
+        assert np.array_equal(got[1], alone[q][1]), f"instance {q}: surface differs"
+        s.close()
+
+
+def test_batch_join_and_leave(gpu_lib):
+    """Instances joining and leaving between calls (continuous batching)."""
+    from phonomena_gb300.batch import Batch
+
+    ref = []
+    for q in range(3):
+        s = _sim(SHAPES[q], 10 + q, "f32k", 60)
+        s.step(50)
+        ref.append(_state(s))
+        s.close()
+    sims = [_sim(SHAPES[q], 10 + q, "f32k", 60) for q in range(3)]
+    with Batch(2, precision="f32k") as b:
+        s0 = b.add(sims[0], 50)
+        b.step(20)
+        s1 = b.add(sims[1], 50)
+        b.step(30)  # instance 0 finishes
+        b.sync()
+        assert b.remaining(s0) == 0
+        b.remove(s0)
+        s2 = b.add(sims[2], 50)  # reuses the freed slot
+        b.step(12)
+        b.step(40)
+        b.sync()
+        assert b.remaining(s1) == 0 and b.remaining(s2) == 0
+    for q, s in enumerate(sims):
+        got = _state(s)
+        for a, e in zip(got[0], ref[q][0]):
+            assert np.array_equal(a, e)
+        assert np.array_equal(got[1], ref[q][1])
+        s.close()
+
+
+def test_batch_rejects_mismatched_instances(gpu_lib):
+    from phonomena_gb300._lib import PhonoError
+    from phonomena_gb300.batch import Batch
+
+    with Batch(2, precision="f32k", tile_j=8) as b:
+        s64 = _sim(SHAPES[0], 0, "f64", 10)
+        with pytest.raises(ValueError):
+            b.add(s64, 10)
+        s16 = _sim(SHAPES[0], 0, "f32k", 10, tile_j=16)
+        with pytest.raises(PhonoError, match="tile_j"):
+            b.add(s16, 10)
+        s = _sim(SHAPES[0], 0, "f32k", 10)
+        with pytest.raises(PhonoError, match="source"):
+            b.add(s, 11)
+        for x in (s64, s16, s):
+            x.close()
