@@ -45,7 +45,15 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--fdtd-steps", type=int, default=2000)
+    p.add_argument("--workload", default="crystal", choices=["crystal", "batch", "serve", "precision"],
+                   help="crystal: the 256x256x128 crystal (default); batch: 64 uneven crystals in one persistent "
+                        "launch; serve: Poisson request stream; precision: 1024x1024x256 FP32K vs FP64 error")
+    p.add_argument("--fdtd-steps", type=int, default=None)
+    p.add_argument("--instances", type=int, default=64)
+    p.add_argument("--requests", type=int, default=2000, help="serve: FP32K requests")
+    p.add_argument("--rate", type=float, default=0.0, help="serve: FP32K arrivals per second (0: 70%% load)")
+    p.add_argument("--requests-f64", type=int, default=40, help="serve: plain FP64 requests")
+    p.add_argument("--budget-gb", type=float, default=150.0, help="serve: device memory budget")
     p.add_argument("--cells", default="256,256,128")
     p.add_argument("--tile-j", type=int, default=0)
     p.add_argument("--x-segment", type=int, default=0)
@@ -198,6 +206,280 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def bench_batch(args, rank, world, local, torch, dist):
+    """64 uneven seeded crystals (sizes {64..192}^2 x {32..96} cells, a in
+    {8,12,16}, f ~ U[20, 60] MHz), 1500 steps each, FP32 Kahan, in one
+    persistent launch per time step with a graph-captured step loop; tile
+    height and per-instance x segments from the batch autotuner.  One bench
+    step = the whole batch from the zero state to its last step."""
+    from phonomena_gb300 import autotune, crystal
+    from phonomena_gb300.batch import Batch
+    from phonomena_gb300.device import DeviceSimulation
+
+    S = args.fdtd_steps or 1500
+    specs = crystal.config4_specs(n=args.instances, seed=rank, steps=S)
+    built = [crystal.build(sp) for sp in specs]
+    shapes = [sp.nodes for sp in specs]
+    node_sum = sum(sp.n_nodes for sp in specs)
+    srcs = [crystal.sin_source(sp.freq, m.dt, S) for sp, (g, m) in zip(specs, built)]
+
+    def make(prec, tj, segs):
+        sims = []
+        for (g, m), xs, src in zip(built, segs, srcs):
+            sim = DeviceSimulation(g.spacing(), m.ids, m.table, m.dt, precision=prec, surface_mode="corrected",
+                                   max_steps=S, record_every=10, tile_j=tj, x_segment=xs)
+            sim.set_source(src)
+            sims.append(sim)
+        return sims
+
+    def run_once(b, sims):
+        for s in sims:
+            s.reset()
+        slots = [b.add(s, S) for s in sims]
+        b.step(S)
+        ms = b.last_step_ms()
+        b.sync()
+        for q in slots:
+            b.remove(q)
+        return ms
+
+    tj, segs = autotune.tune_batch(shapes, "f32k")
+    sims = make("f32k", tj, segs)
+    batch = Batch(len(sims), precision="f32k", tile_j=tj)
+    for _ in range(args.warmup):
+        run_once(batch, sims)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    bus = getattr(torch.cuda.get_device_properties(local), "pci_bus_id", "")
+    with ClockSampler(bus) as clk:
+        times = [run_once(batch, sims) for _ in range(args.steps)]
+    ms = sum(times)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    clocks = clk.summary()
+    value = world * node_sum * S * args.steps / (ms / 1e3) / 1e9
+    surf32 = [s.read_surface().astype(np.float64) for s in sims]
+
+    # the same instances one after another, each alone on its own handle
+    seq_ms = 0.0
+    for s in sims:
+        s.reset()
+        s.step(S)
+        s.sync()
+        seq_ms += s.last_step_ms()
+    same = all(np.array_equal(s.read_surface().astype(np.float64), r) for s, r in zip(sims, surf32))
+
+    # e2e: per bench step, materials and sources host->device, the batch run,
+    # every instance's surface records device->host (pinned buffers)
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+    ids_h = [pinned(m.ids.shape, torch.uint8) for g, m in built]
+    src_h = [pinned((S,), torch.float64) for _ in built]
+    surf_h = [pinned((S // 10, sh[0], sh[1]), torch.float32) for sh in shapes]
+    for (g, m), a, b_, src in zip(built, ids_h, src_h, srcs):
+        a[...] = m.ids
+        b_[...] = src
+    h2d = sum(a.nbytes + b_.nbytes + m.table.nbytes for a, b_, (g, m) in zip(ids_h, src_h, built))
+    d2h = sum(x.nbytes for x in surf_h)
+
+    def e2e_once():
+        for s, a, b_, (g, m) in zip(sims, ids_h, src_h, built):
+            s.set_materials(a, m.table)
+            s.set_source(b_)
+            s.reset()
+        slots = [batch.add(s, S) for s in sims]
+        batch.step(S)
+        batch.sync()
+        for s, out in zip(sims, surf_h):
+            s.read_surface(0, S // 10, out=out)
+        for q in slots:
+            batch.remove(q)
+
+    e2e_once()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_once()
+    wall = time.perf_counter() - t0
+    e2e = world * node_sum * S * args.steps / wall / 1e9
+    batch.close()
+    for s in sims:
+        s.close()
+
+    # plain FP64 batch of the same instances, one run: throughput and error
+    tj64, segs64 = autotune.tune_batch(shapes, "f64", steps=4, tile_js=(8, 16))
+    sims64 = make("f64", tj64, segs64)
+    b64 = Batch(len(sims64), precision="f64", tile_j=tj64)
+    ms64 = run_once(b64, sims64)
+    errs = []
+    for s, r in zip(sims64, surf32):
+        ref = s.read_surface()
+        errs.append(float(np.linalg.norm(r - ref) / np.linalg.norm(ref)))
+    b64.close()
+    for s in sims64:
+        s.close()
+
+    launch_ms = ms / (args.steps * S)
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_NODE * node_sum / (launch_ms / 1e3) / 1e9
+    tpn = traffic_per_node("batch_step_kernel_f32k")
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded crystals)",
+            "config": {"workload": f"batch of {len(specs)} uneven crystals ({node_sum} nodes in all), {S} time steps "
+                                   "each, one persistent launch per time step, graph-captured step loop, FP32 Kahan",
+                       "instances": len(specs), "nodes": node_sum, "fdtd_steps": S,
+                       "tile_j": tj, "x_segment_by_instance": segs,
+                       "l2": f"inputs larger than L2 (state {node_sum * 72 / 1e9:.1f} GB)",
+                       "parallelism": f"replicas x{world}"},
+            "sequential": {"value": round(world * node_sum * S / (seq_ms / 1e3) / 1e9, 4), "unit": "Gcell-updates/s",
+                           "ms": round(seq_ms, 3), "speedup_batch_over_sequential":
+                               round(seq_ms / (ms / args.steps), 3), "bit_identical_to_batch": bool(same)},
+            "fp64": {"value": round(world * node_sum * S / (ms64 / 1e3) / 1e9, 4), "unit": "Gcell-updates/s",
+                     "ms": round(ms64, 3), "speedup_f32k_over_f64": round(ms64 / (ms / args.steps), 3),
+                     "tile_j": tj64},
+            "error_vs_fp64": {"rel_l2_surface_uz_max": max(errs), "rel_l2_surface_uz_median": float(np.median(errs)),
+                              "fdtd_steps": S},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
+                         "traffic": (round(tpn * node_sum) if tpn else None),
+                         "algorithmic_bytes_per_launch": BYTES_PER_NODE * node_sum,
+                         "avg_launch_ms": round(launch_ms, 5),
+                         "launch_timing": "one time step = persistent tile launch + batched face launch "
+                                          "(+1/12 counter update); the whole step is charged to the stencil kernel"},
+            "cpu_baseline": None,
+            "e2e": {"value": round(e2e, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": graph_launches(S, True) * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def bench_serve(args, rank, world, local, torch, dist):
+    """Poisson stream of crystal-simulation requests (config-4 size mix plus
+    5% 512x512x128-cell jobs, 500-3000 steps each, surface uz every 10
+    steps) served by continuous batching under a device-memory budget; FP32K
+    and plain FP64 streams, each at about 70% of its own throughput."""
+    from phonomena_gb300 import serve
+
+    budget = args.budget_gb * 1e9
+    gcell32, gcell64 = 28.0, 1.3  # batched throughputs used to set the default rates
+    rate32 = args.rate or serve.rate_for_load(gcell32, 0.7)
+    rate64 = rate32 * gcell64 / gcell32
+
+    def run(precision, n, rate, seed):
+        reqs = serve.poisson_stream(n, rate, seed=seed)
+        be = serve.GpuBackend(precision=precision, capacity=256, max_steps=3000)
+        srv = serve.Server(be, budget_bytes=budget, capacity=256, chunk=60)
+        streamed = []
+        srv.on_result = lambda r: streamed.append(r.surface.nbytes)
+        t0 = time.perf_counter()
+        res = srv.run(reqs, realtime=True)
+        wall = time.perf_counter() - t0
+        srv.close()
+        be.close()
+        out = serve.summarize(res)
+        out.update({"rate_per_s": round(rate, 4), "offered_gcell_per_s": round(rate * serve.mean_work() / 1e9, 3),
+                    "wall_s": round(wall, 2), "peak_resident_gb": round(srv.stats.peak_bytes / 1e9, 2),
+                    "peak_active": srv.stats.peak_active, "chunks": srv.stats.chunks,
+                    "rejected": len(srv.stats.rejected), "streamed_surface_bytes": int(sum(streamed))})
+        return out
+
+    bus = getattr(torch.cuda.get_device_properties(local), "pci_bus_id", "")
+    with ClockSampler(bus) as clk:
+        r32 = run("f32k", args.requests, rate32, seed=rank)
+    clocks = clk.summary()
+    r64 = run("f64", args.requests_f64, rate64, seed=rank + 1000)
+    if rank == 0:
+        line = {
+            "metric": "served Gcell-updates/s", "value": round(r32["gcell_updates_per_s"], 4),
+            "unit": "Gcell-updates/s", "n_gpus": world, "steps": 1, "warmup": 0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded request stream)",
+            "config": {"workload": f"Poisson stream of {args.requests} requests at {rate32:.3f}/s (70% of "
+                                   f"{gcell32} Gcell/s offered), sizes {{64..192}}^2 x {{32..96}} cells plus 5% "
+                                   "512x512x128, 500-3000 steps, uz surface every 10 steps, "
+                                   f"{args.budget_gb:.0f} GB device budget, continuous batching",
+                       "parallelism": f"replicas x{world}"},
+            "latency_s": {"p50": round(r32["p50_s"], 4), "p95": round(r32["p95_s"], 4), "p99": round(r32["p99_s"], 4)},
+            "f32k": r32, "fp64": r64, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def bench_precision(args, rank, world, local, torch, dist):
+    """1024x1024x256-cell seeded crystal (config-2 recipe), 4000 steps: FP32
+    fields with Kahan-compensated u against the plain FP64 path (the
+    reference arithmetic) on the same inputs; relative L2 error of surface
+    uz and of the total energy after 1000, 2000 and 4000 steps, and the
+    throughput of both runs."""
+    from phonomena_gb300 import autotune
+    from phonomena_gb300.device import DeviceSimulation
+
+    cells = (1024, 1024, 256) if args.cells == "256,256,128" else tuple(int(c) for c in args.cells.split(","))
+    S = args.fdtd_steps or 4000
+    marks = [m for m in (S // 4, S // 2, S) if m > 0]
+    spec, g, m, src = workload(cells, rank, S)
+    sp = g.spacing()
+    every = S // 4
+
+    def run(prec):
+        tj, xs = autotune.tune(sp, m.ids, m.table, m.dt, precision=prec,
+                               candidates=None if prec == "f32k" else [(8, 32), (16, 32)])
+        sim = DeviceSimulation(sp, m.ids, m.table, m.dt, precision=prec, surface_mode="corrected", max_steps=S,
+                               record_every=every, tile_j=tj, x_segment=xs)
+        sim.set_source(src)
+        stream = torch.cuda.ExternalStream(sim.stream_ptr)
+        energy, ms, done = {}, 0.0, 0
+        for mk in marks:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim.step(mk - done)
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            done = mk
+            energy[mk] = sum(sim.energy())
+        sim.sync()
+        surf = sim.read_surface()
+        sim.close()
+        return {"ms": ms, "energy": energy, "surf": surf, "tile": [tj, xs]}
+
+    r32 = run("f32k")
+    r64 = run("f64")
+    per = {}
+    for mk in marks:
+        rec = mk // every - 1
+        a, b = r32["surf"][rec].astype(np.float64), r64["surf"][rec]
+        per[str(mk)] = {"rel_l2_surface_uz": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                        "rel_energy": float(abs(r32["energy"][mk] - r64["energy"][mk]) / abs(r64["energy"][mk])),
+                        "energy_f64": r64["energy"][mk]}
+    nodes = spec.n_nodes
+    v32 = nodes * S / (r32["ms"] / 1e3) / 1e9
+    v64 = nodes * S / (r64["ms"] / 1e3) / 1e9
+    if rank == 0:
+        line = {"metric": "rel L2 error FP32K vs FP64", "value": max(v["rel_l2_surface_uz"] for v in per.values()),
+                "unit": "relative L2", "higher_is_better": False, "n_gpus": world, "steps": 1, "warmup": 0,
+                "dtype": "f32", "data": "synthetic (seeded crystal)",
+                "config": {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({nodes} nodes), {S} time "
+                                       "steps, FP32K vs plain FP64 on the same inputs", "nodes": nodes},
+                "errors_at_step": per,
+                "f32k": {"value": round(v32, 4), "unit": "Gcell-updates/s", "ms": round(r32["ms"], 1),
+                         "tile": r32["tile"]},
+                "fp64": {"value": round(v64, 4), "unit": "Gcell-updates/s", "ms": round(r64["ms"], 1),
+                         "tile": r64["tile"]},
+                "speedup_f32k_over_f64": round(v32 / v64, 3)}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -215,10 +497,16 @@ def main():
     import __graft_entry__
 
     __graft_entry__.build()
+    if args.workload != "crystal":
+        {"batch": bench_batch, "serve": bench_serve, "precision": bench_precision}[args.workload](
+            args, rank, world, local, torch, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     from phonomena_gb300.device import DeviceSimulation
 
     cells = tuple(int(c) for c in args.cells.split(","))
-    S = args.fdtd_steps
+    S = args.fdtd_steps or 2000
     spec, g, m, src = workload(cells, rank, S)
     nodes = spec.n_nodes
     sp = g.spacing()

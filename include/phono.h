@@ -94,6 +94,12 @@ typedef struct phono_desc {
 
 typedef struct phono_handle phono_handle;
 
+/* Device bytes phono_create would allocate for a mesh of nx*ny*nz nodes with
+ * these settings (each allocation rounded up to 512 bytes): what a caller
+ * admitting simulations against a memory budget charges per handle.  No
+ * reference counterpart. */
+int phono_footprint(int nx, int ny, int nz, int precision, int max_steps, int record_every, size_t *bytes);
+
 /* Allocate the device state (zero fields) for one simulation.
  * Replaces BaseSolver.init (base_solver.py:194-222). */
 int phono_create(const phono_desc *desc, phono_handle **out);
@@ -193,9 +199,11 @@ int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *str
  * captured CUDA graph.  The reference runs one simulation per solver object
  * (base_solver.py:245-266) and has no counterpart; the per-instance
  * arithmetic is that of phono_step, bit for bit.  Instances are handles made
- * by phono_create with the batch's precision and tile_j and ny >= 4; while a
- * handle is in a batch, step it only through the batch and call
- * phono_batch_sync before reading it. */
+ * by phono_create with the batch's precision and tile_j and ny >= 4; each
+ * keeps its own x_segment.  While a handle is in a batch, phono_step,
+ * phono_reset, phono_set_materials, phono_upload and phono_set_tiling on it
+ * return PHONO_ERR_STATE; call phono_batch_sync before reading it.  A handle
+ * destroyed while in a batch leaves the batch. */
 typedef struct phono_batch phono_batch;
 
 int phono_batch_create(int capacity, int precision, int tile_j, phono_batch **out);
@@ -209,6 +217,12 @@ int phono_batch_step(phono_batch *b, int nsteps);
 int phono_batch_sync(phono_batch *b);
 int phono_batch_last_step_ms(phono_batch *b, float *ms);
 void phono_batch_destroy(phono_batch *b);
+
+/* Change the tile shape of a handle (0 keeps a value): tile_j rows per block
+ * (4, 8, 16) and x_segment planes per block column.  Results do not depend
+ * on the tile shape; the tuner (phonomena_gb300/autotune.py) calls this to
+ * time candidates on one handle.  No reference counterpart. */
+int phono_set_tiling(phono_handle *h, int tile_j, int x_segment);
 
 /* Device time of the last phono_step call in milliseconds (CUDA events). */
 int phono_last_step_ms(phono_handle *h, float *ms);

@@ -27,7 +27,7 @@ EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
            "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
            "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
-           "phono_batch_destroy",
+           "phono_batch_destroy", "phono_set_tiling", "phono_footprint",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
 
@@ -101,6 +101,8 @@ def load(path: Path | None = None):
         "phono_batch_sync": (ci, [vp]),
         "phono_batch_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_batch_destroy": (None, [vp]),
+        "phono_set_tiling": (ci, [vp, ci, ci]),
+        "phono_footprint": (ci, [ci, ci, ci, ci, ci, ci, ctypes.POINTER(ctypes.c_size_t)]),
         "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_destroy": (None, [vp]),
         "phono_last_error": (ctypes.c_char_p, []),

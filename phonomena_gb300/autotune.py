@@ -1,10 +1,21 @@
-"""Tile-shape autotuner for the fused step kernel.
+"""Tile-shape autotuner for the fused step kernel, single meshes and batches.
 
-For a mesh shape and arithmetic scheme it times every (tile_j, x_segment)
-candidate on the device (CUDA events around a chunk of steps, from the zero
-state, on a scratch simulation of the same shape) and keeps the fastest.  The
-result is cached per (scheme, mesh, device) in a JSON file next to the built
-library, so a shape is tuned once per machine.
+``tune``: for one mesh shape and arithmetic scheme it times every
+(tile_j, x_segment) candidate on a scratch simulation of that shape (CUDA
+events around a chunk of steps from the zero state; ``phono_set_tiling``
+switches the candidate in place) and keeps the fastest.
+
+``tune_batch``: for a mix of mesh shapes stepped as one batch it picks the
+batch's tile height and each instance's x segment, i.e. how many
+(instance, tile) work items every instance contributes to the persistent
+launch.  Stage 1 times the whole mix for every tile height and one common
+x segment; stage 2 revisits the x segment of each group of instances with
+the same x extent, keeping a change only when the whole batch gets faster.
+
+Timing uses scratch simulations (zero material ids and zero source: the
+kernel's work does not depend on the values), so tuning never touches the
+caller's state.  Results are cached per (scheme, shapes, device) in a JSON
+file next to the built library, so a mesh or a mix is tuned once per machine.
 
 tile_j sets the block (32 x tile_j threads, shared memory per block); the
 x segment sets how many x planes a block marches and thereby the number of
@@ -13,6 +24,7 @@ segment).
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 from pathlib import Path
@@ -23,6 +35,7 @@ CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 TILE_J = (4, 8, 16)
 X_SEGMENTS = (16, 24, 32, 40, 48, 64)
 DEFAULT = (8, 32)
+_HOST_ROW = np.array([[224e9, 64e9, 64e9, 64e9, 224e9, 64e9, 64e9, 64e9, 224e9, 80e9, 80e9, 80e9, 2330.0]])
 
 
 def _device_name():
@@ -45,43 +58,125 @@ def _load():
         return {}
 
 
-def _store(d):
+def _store(key, value):
+    d = _load()
+    d[key] = value
     CACHE.parent.mkdir(exist_ok=True)
-    tmp = CACHE.with_suffix(".tmp")
+    tmp = CACHE.with_suffix(f".tmp{os.getpid()}")
     tmp.write_text(json.dumps(d, indent=1, sort_keys=True))
     os.replace(tmp, CACHE)
 
 
-def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None, use_cache=True, verbose=False):
-    """Best (tile_j, x_segment) for this mesh and scheme; times each candidate."""
+def _scratch(shape, precision, max_steps, tile_j=8, x_segment=32):
+    """Simulation of the given mesh shape with zero ids, uniform 10 um spacing and a zero source."""
     from .device import DeviceSimulation
 
+    nx, ny, nz = shape
+    sp = {f"fd{a}": np.full(n - 1, 1e-5) for a, n in zip("xyz", shape)}
+    sp.update({f"sd{a}": np.full(n - 2, 1e-5) for a, n in zip("xyz", shape)})
+    sim = DeviceSimulation(sp, np.zeros(shape, np.uint8), _HOST_ROW, 1e-10, precision=precision,
+                           surface_mode="corrected", max_steps=max_steps, tile_j=tile_j, x_segment=x_segment)
+    sim.set_source(np.zeros(max_steps))
+    return sim
+
+
+def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None, use_cache=True, verbose=False):
+    """Best (tile_j, x_segment) for this mesh and scheme; times each candidate."""
     shape = tuple(int(s) for s in np.shape(mat))
     key = _key(precision, shape)
-    cache = _load() if use_cache else {}
-    if key in cache:
-        return tuple(cache[key]["best"])
+    if use_cache:
+        hit = _load().get(key)
+        if hit:
+            return tuple(hit["best"])
     if steps is None:
         steps = 48 if precision == "f32k" else 12
     cands = candidates or [(tj, xs) for tj in TILE_J for xs in X_SEGMENTS]
-    src = np.zeros(steps + 12)
     results = []
-    for tj, xs in cands:
-        with DeviceSimulation(spacing, mat, table, dt, precision=precision, surface_mode="corrected",
-                              max_steps=steps + 12, tile_j=tj, x_segment=xs) as sim:
-            sim.set_source(src)
-            sim.step(12)  # warm up: graph capture, first-touch
+    sim = _scratch(shape, precision, (steps + 12) * len(cands) + 12)
+    try:
+        for tj, xs in cands:
+            sim.set_tiling(tj, xs)
+            sim.step(12)  # warm up: graph capture
             sim.sync()
             sim.step(steps)
             ms = sim.last_step_ms() / steps
             results.append((ms, tj, xs))
             if verbose:
                 print(f"autotune {precision} {shape} tile_j={tj} x_segment={xs}: {ms:.4f} ms/step")
+    finally:
+        sim.close()
     results.sort()
     best = (results[0][1], results[0][2])
     if use_cache:
-        cache = _load()
-        cache[key] = {"best": list(best), "ms_per_step": results[0][0],
-                      "all": [[tj, xs, round(ms, 5)] for ms, tj, xs in results]}
-        _store(cache)
+        _store(key, {"best": list(best), "ms_per_step": results[0][0],
+                     "all": [[tj, xs, round(ms, 5)] for ms, tj, xs in results]})
     return best
+
+
+def _batch_key(precision, shapes):
+    h = hashlib.sha1(json.dumps(sorted(map(list, shapes))).encode()).hexdigest()[:16]
+    return f"batch:{precision}:{len(shapes)}:{h}:{_device_name()}"
+
+
+def tune_batch(shapes, precision="f32k", steps=24, tile_js=TILE_J, use_cache=True, verbose=False):
+    """Tile height of a batch and the x segment of each instance.
+
+    shapes: mesh node counts (nx, ny, nz) of the instances, in batch order.
+    Returns (tile_j, [x_segment per instance]).
+    """
+    from .batch import Batch
+
+    shapes = [tuple(int(v) for v in s) for s in shapes]
+    key = _batch_key(precision, shapes) + ":" + ",".join(map(str, tile_js))
+    if use_cache:
+        hit = _load().get(key)
+        if hit:
+            by_nx = {int(k): v for k, v in hit["x_segment_by_nx"].items()}
+            return int(hit["tile_j"]), [by_nx[s[0]] for s in shapes]
+    groups = sorted({s[0] for s in shapes})
+    seg_cands = {nx: sorted({xs for xs in X_SEGMENTS if xs < nx - 1} | {nx - 1}) for nx in groups}
+    n_timings = len(tile_js) * (len(X_SEGMENTS) + 1) + sum(len(c) for c in seg_cands.values())
+    budget = (steps + 12) * (n_timings + 2)
+    sims = [_scratch(s, precision, budget) for s in shapes]
+    log = []
+
+    def time_mix(tj, seg_by_nx):
+        for sim in sims:
+            sim.set_tiling(tj, seg_by_nx[sim.nx])
+        with Batch(len(sims), precision=precision, tile_j=tj) as b:
+            for sim in sims:
+                b.add(sim, steps + 12)
+            b.step(12)  # work list upload, graph capture
+            b.sync()
+            b.step(steps)
+            ms = b.last_step_ms() / steps
+        log.append([tj, {str(k): v for k, v in seg_by_nx.items()}, round(ms, 5)])
+        if verbose:
+            print(f"autotune batch tile_j={tj} x_segment={seg_by_nx}: {ms:.4f} ms/step")
+        return ms
+
+    try:
+        best = None
+        for tj in tile_js:
+            for xs in list(X_SEGMENTS) + [0]:  # 0: one segment per block column
+                seg = {nx: (min(xs, nx - 1) if xs else nx - 1) for nx in groups}
+                ms = time_mix(tj, seg)
+                if best is None or ms < best[0]:
+                    best = (ms, tj, dict(seg))
+        ms_best, tj, seg = best
+        for nx in reversed(groups):  # per-group refinement, largest x extent first
+            for xs in seg_cands[nx]:
+                if xs == seg[nx]:
+                    continue
+                trial = dict(seg)
+                trial[nx] = xs
+                ms = time_mix(tj, trial)
+                if ms < 0.99 * ms_best:
+                    ms_best, seg = ms, trial
+    finally:
+        for sim in sims:
+            sim.close()
+    if use_cache:
+        _store(key, {"tile_j": tj, "x_segment_by_nx": {str(k): v for k, v in seg.items()},
+                     "ms_per_step": ms_best, "timings": log})
+    return tj, [seg[s[0]] for s in shapes]

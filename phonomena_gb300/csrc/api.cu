@@ -83,6 +83,7 @@ struct phono_handle {
   int steps_done = 0;
   int nmat = 0;
   bool timed = false;
+  phono_batch* batch = nullptr;  // the batch that steps this handle, if any
 };
 
 static long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
@@ -97,8 +98,11 @@ static int dalloc(phono_handle* h, void** p, size_t bytes) {
   return PHONO_OK;
 }
 
+static void batch_detach(phono_batch* b, const phono_handle* h);
+
 static void release(phono_handle* h) {
   if (!h) return;
+  if (h->batch) batch_detach(h->batch, h);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (void* p : h->allocs) cudaFree(p);
@@ -241,6 +245,36 @@ static cudaError_t launch_one(phono_handle* h, int step_off) {
   return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->separate_faces, h->stream);
 }
 
+// Padded device layout: planes -1..nx, rows -1..ny, a KOFF-element front pad
+// in z and rows rounded up to 128 bytes; material ids with an MKOFF front pad
+// and 16-byte rows.
+static long long field_row(int nz, int es) {
+  const long long koff = es == 8 ? Lay<double>::KOFF : Lay<float>::KOFF;
+  return round_up(koff + nz + 1, 128 / es);
+}
+static long long mat_row(int nz) { return round_up(MKOFF + nz + 1, 16); }
+
+// Bytes of device memory phono_create allocates for a handle (each cudaMalloc
+// rounded up to 512 bytes).
+static size_t handle_bytes(int nx, int ny, int nz, int precision, int max_steps, int record_every) {
+  const int es = precision == PHONO_F32K ? 4 : 8;
+  const int nbuf = precision == PHONO_F64 ? 3 : 2;
+  auto r = [](size_t b) { return (b + 511) / 512 * 512; };
+  const size_t field_elems = (size_t)(nx + 2) * (ny + 2) * field_row(nz, es);
+  const size_t fb = field_elems * es * 3 * nbuf;
+  size_t total = r(fb) * (precision == PHONO_F64 ? 1 : 3);
+  const int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
+  for (int a = 0; a < 6; a++) total += r((size_t)lens[a] * es) + r((size_t)lens[a] * 8);
+  total += r((size_t)(nx + 2) * (ny + 2) * mat_row(nz));
+  total += r((size_t)256 * 16 * es) + r((size_t)256 * PHONO_TABLE_COLS * 8);
+  const int cap = max_steps > 0 ? max_steps : 1;
+  total += r((size_t)cap * 8);
+  const int nrec = record_every > 0 ? max_steps / record_every : 0;
+  if (nrec > 0) total += r((size_t)nrec * nx * ny * es);
+  total += r(sizeof(int) * 2) + r(sizeof(double2) * kEnergyBlocks) + r(sizeof(double) * 2);
+  return total;
+}
+
 static int check_desc(const phono_desc* d) {
   if (!d) return fail(PHONO_ERR_ARG, "desc is NULL");
   if (d->nx < 3 || d->ny < 3 || d->nz < 3) return fail(PHONO_ERR_ARG, "nx, ny, nz must be >= 3 mesh nodes");
@@ -315,6 +349,42 @@ static void* field_ptr(phono_handle* h, int field) {
   return nullptr;
 }
 
+// Tile decomposition of a handle: tile_j rows x 32 z-points per block, the
+// x axis cut into segments of x_segment planes, and the face-pass work list.
+static int set_tiling(phono_handle* h, int tj, int xseg) {
+  const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
+  const int ntj = (ny - 1 + tj - 1) / tj, ntk = (nz - 1 + TK - 1) / TK, nseg = (nx - 1 + xseg - 1) / xseg;
+  long long ntile = (long long)ntj * ntk * nseg;
+  // face points left to the face pass, per component: z=N only where it meets
+  // an x / y face (2*ex + ey-2; the tile pass writes the rest), y=N and y=0
+  // (ex*(ez-1)), x=N ((ey-2)*(ez-1))
+  FaceTable faces{};
+  long long acc = 0;
+  for (int c = 0; c < 3; c++) {
+    long long ex = nx - (c == 0), ey = ny - (c == 1), ez = nz - (c == 2);
+    long long cnt[4] = {2 * ex + (ey - 2), ex * (ez - 1), ex * (ez - 1), (ey - 2) * (ez - 1)};
+    for (int p = 0; p < 4; p++) {
+      faces.off[c * 4 + p] = (int)acc;
+      acc += cnt[p];
+    }
+  }
+  faces.off[12] = (int)acc;
+  const long long nface = (acc + TK * tj - 1) / (TK * tj);
+  if (ntile + nface > 0x7fffffffLL || acc > 0x7fffffffLL) return fail(PHONO_ERR_ARG, "grid too large for one launch");
+  h->tj = tj;
+  h->xseg = xseg;
+  h->ntj = ntj;
+  h->ntk = ntk;
+  h->nseg = nseg;
+  h->faces = faces;
+  h->n_tile = (int)ntile;
+  h->n_face = (int)nface;
+  // faces in a second launch that reads the tile pass's interior values; the
+  // chain end of a face point can itself be a face point only when ny == 3
+  h->separate_faces = ny >= 4 ? 1 : 0;
+  return PHONO_OK;
+}
+
 // TMA descriptors: a 4-D (k, j, i, array) map over the u allocation with a
 // (KW, TJ+2, 1, 3) box (one plane tile of the three components of a buffer)
 // and a 3-D (k, j, i) map over the material ids with a (48, TJ+2, 1) box.
@@ -352,6 +422,17 @@ extern "C" {
 
 int phono_abi_version(void) { return PHONO_ABI_VERSION; }
 
+int phono_footprint(int nx, int ny, int nz, int precision, int max_steps, int record_every, size_t* bytes) {
+  if (!bytes) return fail(PHONO_ERR_ARG, "bytes is NULL");
+  if (nx < 3 || ny < 3 || nz < 3) return fail(PHONO_ERR_ARG, "nx, ny, nz must be >= 3 mesh nodes");
+  if ((long long)nx * ny * nz > (1LL << 34)) return fail(PHONO_ERR_ARG, "grid too large");
+  if (precision != PHONO_F64 && precision != PHONO_F32K && precision != PHONO_F64V)
+    return fail(PHONO_ERR_ARG, "unknown precision");
+  if (max_steps < 0 || record_every < 0) return fail(PHONO_ERR_ARG, "max_steps and record_every must be >= 0");
+  *bytes = handle_bytes(nx, ny, nz, precision, max_steps, record_every);
+  return PHONO_OK;
+}
+
 const char* phono_last_error(void) { return g_err.c_str(); }
 
 int phono_create(const phono_desc* d, phono_handle** out) {
@@ -369,7 +450,7 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   const int nx = d->nx, ny = d->ny, nz = d->nz;
   // padded layout: planes -1..nx, rows -1..ny, 32-byte front pad in z
   const long long koff = h->es == 8 ? Lay<double>::KOFF : Lay<float>::KOFF;
-  const long long pz = round_up(koff + nz + 1, 128 / h->es);
+  const long long pz = field_row(nz, h->es);
   h->nbuf = f64 ? 3 : 2;
   h->g.nx = nx;
   h->g.ny = ny;
@@ -379,43 +460,19 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->g.o0 = h->g.sx + h->g.sy + koff;
   h->field_elems = (size_t)(nx + 2) * h->g.sx;
   h->g.fstride = (long long)h->field_elems;
-  const long long mpz = round_up(MKOFF + nz + 1, 16);
+  const long long mpz = mat_row(nz);
   h->g.msy = mpz;
   h->g.msx = (long long)(ny + 2) * mpz;
   h->g.mo0 = h->g.msx + h->g.msy + MKOFF;
   h->mat_bytes = (size_t)(nx + 2) * h->g.msx;
 
   // tiles
-  h->tj = d->tile_j ? d->tile_j : 8;
-  h->xseg = d->x_segment ? d->x_segment : 32;
-  h->ntj = (ny - 1 + h->tj - 1) / h->tj;
-  h->ntk = (nz - 1 + TK - 1) / TK;
-  h->nseg = (nx - 1 + h->xseg - 1) / h->xseg;
-  long long ntile = (long long)h->ntj * h->ntk * h->nseg;
-  // face points left to the face pass, per component: z=N only where it meets
-  // an x / y face (2*ex + ey-2; the tile pass writes the rest), y=N and y=0
-  // (ex*(ez-1)), x=N ((ey-2)*(ez-1))
-  long long acc = 0;
-  for (int c = 0; c < 3; c++) {
-    long long ex = nx - (c == 0), ey = ny - (c == 1), ez = nz - (c == 2);
-    long long cnt[4] = {2 * ex + (ey - 2), ex * (ez - 1), ex * (ez - 1), (ey - 2) * (ez - 1)};
-    for (int p = 0; p < 4; p++) {
-      h->faces.off[c * 4 + p] = (int)acc;
-      acc += cnt[p];
-    }
-  }
-  h->faces.off[12] = (int)acc;
-  int nt = TK * h->tj;
-  long long nface = (acc + nt - 1) / nt;
-  // faces in a second launch that reads the tile pass's interior values; the
-  // chain end of a face point can itself be a face point only when ny == 3
-  h->separate_faces = ny >= 4 ? 1 : 0;
-  if (ntile + nface > 0x7fffffffLL || acc > 0x7fffffffLL) {
+  if (set_tiling(h, d->tile_j ? d->tile_j : 8, d->x_segment ? d->x_segment : 32)) {
+    std::string m_ = g_err;
     delete h;
-    return fail(PHONO_ERR_ARG, "grid too large for one launch");
+    g_err = m_;
+    return PHONO_ERR_ARG;
   }
-  h->n_tile = (int)ntile;
-  h->n_face = (int)nface;
 
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -538,6 +595,7 @@ static int build_graph(phono_handle* h) {
 
 int phono_step(phono_handle* h, int nsteps) {
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch: step it with phono_batch_step");
   if (nsteps < 0) return fail(PHONO_ERR_ARG, "nsteps < 0");
   if (h->steps_done + nsteps > h->nsrc)
     return fail(PHONO_ERR_STATE, "not enough source samples: call phono_set_source with max_steps samples");
@@ -611,6 +669,7 @@ int phono_download(phono_handle* h, int field, void* host, size_t bytes) {
 }
 
 int phono_upload(phono_handle* h, int field, const void* host, size_t bytes) {
+  if (h && h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
   void* dev;
   int rc = field_check(h, field, host, bytes, &dev);
   if (rc) return rc;
@@ -651,6 +710,7 @@ int phono_energy(phono_handle* h, double out[2]) {
 
 int phono_reset(phono_handle* h) {
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
   const size_t fb = h->field_elems * h->es * 3 * h->nbuf;
   CK(cudaMemsetAsync(h->ubase, 0, fb, h->stream));
   if (h->vbase) CK(cudaMemsetAsync(h->vbase, 0, fb, h->stream));
@@ -663,6 +723,7 @@ int phono_reset(phono_handle* h) {
 
 int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table, int nmat) {
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
   int rc = check_materials(h, mat, table, nmat);
   if (rc) return rc;
   rc = upload_materials(h, mat, table, nmat);
@@ -677,6 +738,35 @@ int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table
 }
 
 void* phono_stream(phono_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int phono_set_tiling(phono_handle* h, int tile_j, int x_segment) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (tile_j == 0) tile_j = h->tj;
+  if (x_segment == 0) x_segment = h->xseg;
+  if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
+  if (x_segment < 0) return fail(PHONO_ERR_ARG, "x_segment must be >= 0");
+  if (tile_j == h->tj && x_segment == h->xseg) return PHONO_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  const int p = h->d.precision;
+  CK(p == PHONO_F64 ? configure_step_f64(tile_j)
+                    : (p == PHONO_F64V ? configure_step_f64v(tile_j) : configure_step_f32k(tile_j)));
+  const int old_tj = h->tj, old_xs = h->xseg;
+  int rc = set_tiling(h, tile_j, x_segment);
+  if (!rc) rc = encode_tensor_maps(h);
+  if (rc) {
+    std::string m = g_err;
+    set_tiling(h, old_tj, old_xs);
+    encode_tensor_maps(h);
+    g_err = m;
+    return rc;
+  }
+  if (h->graph) {  // the captured launches hold the old grid and tensor maps
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return PHONO_OK;
+}
 
 void phono_destroy(phono_handle* h) { release(h); }
 
@@ -706,9 +796,23 @@ struct phono_batch {
   int grid_tiles = 0, grid_faces = 0;
 };
 
+// a handle destroyed while in a batch leaves it (the batch's work list is
+// rebuilt before its next step)
+static void batch_detach(phono_batch* b, const phono_handle* h) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (int s = 0; s < b->cap; s++)
+    if (b->slot[s] == h) {
+      b->slot[s] = nullptr;
+      b->remaining[s] = 0;
+      b->dirty = true;
+    }
+}
+
 static void batch_release(phono_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (phono_handle* h : b->slot)
+    if (h) h->batch = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (void* p : b->allocs) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -859,6 +963,7 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** ou
 
 int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
   if (!b || !h) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_ARG, h->batch == b ? "handle already in the batch" : "handle is in another batch");
   if (h->d.precision != b->precision) return fail(PHONO_ERR_ARG, "handle precision differs from the batch");
   if (h->tj != b->tj) return fail(PHONO_ERR_ARG, "handle tile_j differs from the batch");
   if (!h->separate_faces) return fail(PHONO_ERR_ARG, "batched instances need ny >= 4");
@@ -884,12 +989,14 @@ int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
   b->slot[s] = h;
   b->remaining[s] = nsteps;
   b->dirty = true;
+  h->batch = b;
   return s;
 }
 
 int phono_batch_remove(phono_batch* b, int s) {
   if (!b || s < 0 || s >= b->cap || !b->slot[s]) return fail(PHONO_ERR_ARG, "no instance in that slot");
   CK(cudaStreamSynchronize(b->stream));
+  b->slot[s]->batch = nullptr;
   b->slot[s] = nullptr;
   b->remaining[s] = 0;
   b->dirty = true;

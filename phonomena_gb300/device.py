@@ -20,6 +20,16 @@ def field_shape(nx, ny, nz, comp):
     return (nx - (comp == 0), ny - (comp == 1), nz - (comp == 2))
 
 
+def footprint(shape, precision="f32k", max_steps=0, record_every=0):
+    """Device bytes a DeviceSimulation of this mesh shape allocates (phono_footprint)."""
+    L = _lib.load()
+    out = ctypes.c_size_t()
+    nx, ny, nz = (int(v) for v in shape)
+    check(L.phono_footprint(nx, ny, nz, _lib.PRECISIONS[precision], int(max_steps), int(record_every),
+                            ctypes.byref(out)))
+    return int(out.value)
+
+
 class DeviceSimulation:
     """Device-resident FDTD state behind ``phono_create`` / ``phono_step``.
 
@@ -57,6 +67,8 @@ class DeviceSimulation:
         h = ctypes.c_void_p()
         check(L.phono_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
+        self.tile_j = int(tile_j) or 8
+        self.x_segment = int(x_segment) or 32
 
     # -- control ----------------------------------------------------------
     def set_source(self, samples):
@@ -77,6 +89,12 @@ class DeviceSimulation:
         t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 13)
         check(self._L.phono_set_materials(self._h, m.ctypes.data, t.ctypes.data, t.shape[0]))
         self.mat, self.table = m, t
+
+    def set_tiling(self, tile_j=0, x_segment=0):
+        """Change the tile shape (0 keeps a value); results do not depend on it."""
+        check(self._L.phono_set_tiling(self._h, int(tile_j), int(x_segment)))
+        self.tile_j = int(tile_j) or self.tile_j
+        self.x_segment = int(x_segment) or self.x_segment
 
     @property
     def stream_ptr(self):

@@ -104,3 +104,59 @@ def test_batch_rejects_mismatched_instances(gpu_lib):
             b.add(s, 11)
         for x in (s64, s16, s):
             x.close()
+
+
+def test_set_tiling_keeps_results(gpu_lib):
+    """Changing the tile shape mid-run changes nothing in the results."""
+    ref = _sim(SHAPES[2], 3, "f32k", 60)
+    ref.step(60)
+    want = _state(ref)
+    ref.close()
+    s = _sim(SHAPES[2], 3, "f32k", 60)
+    s.step(17)
+    s.set_tiling(16, 24)
+    s.step(25)
+    s.set_tiling(4, 0)
+    s.step(18)
+    got = _state(s)
+    for a, e in zip(got[0], want[0]):
+        assert np.array_equal(a, e)
+    assert np.array_equal(got[1], want[1])
+    s.close()
+
+
+def test_handle_in_batch_is_guarded(gpu_lib):
+    from phonomena_gb300._lib import PhonoError
+    from phonomena_gb300.batch import Batch
+
+    s = _sim(SHAPES[0], 0, "f32k", 24)
+    b = Batch(2, precision="f32k")
+    slot = b.add(s, 24)
+    for call in (lambda: s.step(1), s.reset, lambda: s.set_tiling(4, 16), lambda: b.add(s, 1)):
+        with pytest.raises(PhonoError):
+            call()
+    b.step(24)
+    b.sync()
+    b.remove(slot)
+    s.reset()  # allowed again once out of the batch
+    slot = b.add(s, 24)
+    s.close()  # a handle destroyed while in the batch leaves it
+    b.step(12)
+    b.sync()
+    b.close()
+
+
+def test_footprint_matches_device_allocation(gpu_lib):
+    import torch
+
+    from phonomena_gb300.device import footprint
+
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    s = _sim((120, 100, 60), 1, "f32k", 200)
+    free1 = torch.cuda.mem_get_info()[0]
+    want = footprint((121, 101, 61), "f32k", 200, 5)
+    used = free0 - free1
+    # cudaMalloc reserves whole pages: allow 2 MiB per allocation
+    assert want <= used + (1 << 20) and used - want < 24 * (2 << 20), (used, want)
+    s.close()

@@ -134,3 +134,26 @@ def test_output_npz_schema(tmp_path):
     assert attrs["dt_record"] == m.dt * 2
     for k in ("x", "y", "z", "sdx", "fdz", "steps", "dt", "prim_material", "sec_material", "solver_cfg"):
         assert k in attrs
+
+
+def test_footprint_is_the_padded_layout():
+    """phono_footprint (host only, no device call) against the padded layout:
+    planes -1..nx, rows -1..ny, z rows of 128 bytes after an 8-float front pad."""
+    from phonomena_gb300.device import footprint
+
+    def r(b):
+        return (b + 511) // 512 * 512
+
+    nx, ny, nz, steps, rec = 30, 20, 10, 100, 10
+    row = -(-(8 + nz + 1) // 32) * 32  # floats per z row
+    fe = (nx + 2) * (ny + 2) * row
+    want = 3 * r(fe * 4 * 3 * 2)  # u (2 buffers), v, c: three components each
+    for n in (nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2):
+        want += r(n * 4) + r(n * 8)
+    want += r((nx + 2) * (ny + 2) * (-(-(8 + nz + 1) // 16) * 16))  # ids
+    want += r(256 * 16 * 4) + r(256 * 13 * 8) + r(steps * 8) + r(steps // rec * nx * ny * 4)
+    want += r(8) + r(16 * 1024) + r(16)
+    assert footprint((nx, ny, nz), "f32k", steps, rec) == want
+    assert footprint((nx, ny, nz), "f64", steps, 0) < footprint((nx, ny, nz), "f64v", steps, 0)
+    with pytest.raises(Exception):
+        footprint((2, 5, 5), "f32k", 10, 1)
