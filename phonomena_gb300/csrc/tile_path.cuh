@@ -198,8 +198,16 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   if (want_y(ib)) pwy = load_pw<S>(r, 1, off_j + (long long)ib * g.sx);
   if (want_z(ib)) pwz = load_pw<S>(r, 2, off_j + (long long)ib * g.sx);
 
+  // x spacings of plane p: fdx[p] (T5, T6 at p; ux at p+1) and sdx[p-1]
+  // (T1..T3 at p; uy, uz at p), read one plane ahead so that their latency
+  // is not on the path of the stress evaluation
+  auto fx_at = [&](int p) { return p >= 0 && p <= nx - 2 ? __ldg(a.sp.fdx + p) : R(1); };
+  auto sx_at = [&](int p) { return p >= 1 && p <= nx - 2 ? __ldg(a.sp.sdx + p - 1) : R(1); };
+  R fx_prev = fx_at(ib - 1), fx_cur = fx_at(ib), sx_cur = sx_at(ib);
+
   for (int i = ib; i <= ie; i++) {
     const long long off_i = off_j + (long long)i * g.sx;  // (i, j, k)
+    const R fx_next = fx_at(i + 1), sx_next = sx_at(i + 1);
     Pw<R> nx_{0, 0}, ny_{0, 0}, nz_{0, 0};
     if (want_x(i + 1)) nx_ = load_pw<S>(r, 0, off_i);
     if (want_y(i + 1)) ny_ = load_pw<S>(r, 1, off_i + g.sx);
@@ -207,9 +215,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     // per-plane (uniform) predicates and spacings
     const bool i_n = i >= 1 && i <= nx - 2;  // T1..T4
     const bool i_s = i <= nx - 2;            // T5, T6 (i >= 0 here)
-    const R fdx_i = i_s ? __ldg(a.sp.fdx + i) : R(1);
-    const R sdx_im = i_n ? __ldg(a.sp.sdx + i - 1) : R(1);
-    const R fdx_im = i >= 1 ? __ldg(a.sp.fdx + i - 1) : R(1);
+    const R fdx_i = fx_cur, sdx_im = sx_cur, fdx_im = fx_prev;
     wait_plane(i + 1);
     if (__syncthreads_or(!ok)) break;
     const int p = i & 1;
@@ -360,6 +366,9 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     t1m = t1c;
     t5m = t5c;
     t6m = t6c;
+    fx_prev = fx_cur;
+    fx_cur = fx_next;
+    sx_cur = sx_next;
     uxm = uxc;
     uxm_up = uxc_up;
     pwx = nx_;
