@@ -58,7 +58,7 @@ struct phono_handle {
   char* ubase = nullptr;   // nbuf x 3 padded arrays, buffer-major
   char* vbase = nullptr;   // F32K: 2 x 3 velocity arrays
   char* cbase = nullptr;   // F32K: 2 x 3 Kahan arrays
-  CUtensorMap tm_u{}, tm_mat{};
+  CUtensorMap tm_u{}, tm_mat{}, tm_pw0{}, tm_pw1{};
   void* sp[6] = {};       // R spacings (F64 raw, F32K reciprocals)
   double* sp64[6] = {};   // raw double spacings (energy)
   double h_sp0[6] = {};   // first elements (raw)
@@ -212,6 +212,8 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.src = h->src;
   a.tm_u = h->tm_u;
   a.tm_mat = h->tm_mat;
+  a.tm_pw0 = h->tm_pw0;
+  a.tm_pw1 = h->tm_pw1;
   a.nmat = h->nmat;
   a.ubase = (R*)h->ubase;
   a.vbase = (R*)h->vbase;
@@ -415,6 +417,18 @@ static int encode_tensor_maps(phono_handle* h) {
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PHONO_ERR_CUDA, "cuTensorMapEncodeTiled (materials) failed: " + std::to_string(r));
+  // pointwise state, own points only: a (32, TJ, 1, 3) box over u_old (F64)
+  // or over v and the Kahan terms (velocity forms)
+  cuuint32_t pbox[4] = {(cuuint32_t)TK, (cuuint32_t)h->tj, 1, 3};
+  const bool f64 = h->d.precision == PHONO_F64;
+  void* pw[2] = {f64 ? h->ubase : h->vbase, f64 ? h->ubase : h->cbase};
+  CUtensorMap* maps[2] = {&h->tm_pw0, &h->tm_pw1};
+  for (int q = 0; q < 2; q++) {
+    r = encode(maps[q], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pw[q], dims,
+               strides, pbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(PHONO_ERR_CUDA, "cuTensorMapEncodeTiled (pointwise) failed: " + std::to_string(r));
+  }
   return PHONO_OK;
 }
 
@@ -967,6 +981,8 @@ int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
   if (h->d.precision != b->precision) return fail(PHONO_ERR_ARG, "handle precision differs from the batch");
   if (h->tj != b->tj) return fail(PHONO_ERR_ARG, "handle tile_j differs from the batch");
   if (!h->separate_faces) return fail(PHONO_ERR_ARG, "batched instances need ny >= 4");
+  if (h->nmat > BATCH_TAB_ROWS)
+    return fail(PHONO_ERR_ARG, "batched instances hold at most " + std::to_string(BATCH_TAB_ROWS) + " materials");
   if (nsteps < 0 || h->steps_done + nsteps > h->nsrc)
     return fail(PHONO_ERR_STATE, "not enough source samples for the requested steps");
   int s = -1;

@@ -30,7 +30,8 @@ constexpr int TK = 32;      // tile width along z (the contiguous axis): one war
 constexpr int NSLOT = 4;    // planes in the shared-memory ring
 constexpr int MKOFF = 8;    // material front pad in k (bytes)
 constexpr int MKW = 48;     // material tile width in k (bytes): k0-8 .. k0+40
-constexpr int TAB_SMEM = 256;  // material rows staged in shared memory (all ids)
+constexpr int TAB_ROWS_MAX = 256;  // material rows a table may hold (uint8 ids)
+constexpr int BATCH_TAB_ROWS = 32;  // material rows of a batched instance
 
 template <class R>
 struct Lay;
@@ -77,6 +78,8 @@ template <class R>
 struct StepArgs {
   CUtensorMap tm_u;    // 4-D (k, j, i, buffer*3+component) map of the u allocation
   CUtensorMap tm_mat;  // 3-D (k, j, i) map of the material ids
+  CUtensorMap tm_pw0;  // own-point tiles of u_old (F64) or v (velocity forms), same layout as tm_u
+  CUtensorMap tm_pw1;  // own-point tiles of the Kahan terms (velocity forms)
   Geo g;
   Spacing<R> sp;
   const uint8_t* __restrict__ mat;

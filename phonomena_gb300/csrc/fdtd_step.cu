@@ -560,18 +560,31 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
-template <class R, int TJ>
+// Shared memory of a tile block: mbarriers, the u ring (NSLOT planes of the
+// three components with a 1-node halo), the pointwise ring (own points of
+// u_old, or of v and the Kahan terms, for the same planes), the material-id
+// ring, the stress planes and, last, the material table (its size depends on
+// the number of materials, so it is the only variable part).
+template <class S, int TJ>
 struct SmemPlan {
+  using R = typename S::R;
   using TF = TileFetch<R, TJ>;
   static constexpr int W = TK + 2, PL = W * (TJ + 2);
+  static constexpr int NPW = S::kahan ? 2 : 1;  // pointwise arrays: v and c, or u_old
+  static constexpr int PWC = TJ * TK;           // one component of a pointwise tile
+  static constexpr int PWS = NPW * 3 * PWC;     // one pointwise slot
   static constexpr size_t BARS = 128;
-  static constexpr size_t TAB = TAB_SMEM * 16 * sizeof(R);
   static constexpr size_t UR = (size_t)NSLOT * TF::SU * sizeof(R);
+  static constexpr size_t PWR = (size_t)NSLOT * PWS * sizeof(R);
   static constexpr size_t MR = (size_t)NSLOT * TF::SM;
   static constexpr size_t TS = ((7 * PL * sizeof(R) + 127) / 128) * 128;
-  static constexpr size_t off_tab = BARS, off_u = off_tab + TAB, off_m = off_u + UR, off_t = off_m + MR;
-  static constexpr size_t total = off_t + TS + 128;  // + alignment slack
+  static constexpr size_t off_u = BARS, off_pw = off_u + UR, off_m = off_pw + PWR, off_t = off_m + MR;
+  static constexpr size_t off_tab = off_t + TS;
+  static constexpr size_t fixed = off_tab + 128;  // + alignment slack
+  static constexpr size_t bytes(int table_rows) { return fixed + (size_t)table_rows * 16 * sizeof(R); }
   static constexpr uint32_t tx_bytes = (uint32_t)(3 * (TJ + 2) * Lay<R>::KW * sizeof(R) + (TJ + 2) * MKW);
+  static constexpr uint32_t pw_bytes = (uint32_t)(PWS * sizeof(R));
+  static_assert((PWC * sizeof(R)) % 128 == 0 && (TF::SU * sizeof(R)) % 128 == 0, "ring tiles must stay 128-byte aligned");
 };
 
 #include "tile_path.cuh"
@@ -584,17 +597,12 @@ template <class S, int TJ>
 __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : (TJ < 16 ? 16 / TJ : 1)))
     fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
-  using P = SmemPlan<R, TJ>;
-  using TF = TileFetch<R, TJ>;
-  constexpr int NT = TK * TJ;
-  constexpr int W = P::W, PL = P::PL;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // 128-byte aligned start, derived by pointer arithmetic on the shared array
   // so that every access below stays a shared-memory access (an integer
   // round trip would turn them into generic loads)
   unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
-  const Geo& g = a.g;
   const int tt = __ldg(a.step_base) + a.step_off;
   const Roles<R> r = roles<S>(a, tt);
   const R s = (R)__ldg(a.src + tt);
@@ -602,31 +610,21 @@ __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ 
 
   if ((int)blockIdx.x >= a.n_tile_blocks) {
     // ---------------- face blocks (fused launch) ----------------
-    face_point<S>(a, r, s, tt, ((int)blockIdx.x - a.n_tile_blocks) * NT + tid, false);
+    face_point<S>(a, r, s, tt, ((int)blockIdx.x - a.n_tile_blocks) * (TK * TJ) + tid, false);
     return;
   }
 
   // ---------------- tile blocks ----------------
-  tile_block<S, TJ>(a, base, r, s, tt, tid, blockIdx.x, &a.tm_u, &a.tm_mat);
+  tile_block<S, TJ>(a, base, r, s, tt, tid, blockIdx.x, &a);
 }
 
 // ---------------------------------------------------------------------------
 // host-side launch helpers (called by the C ABI in api.cu)
 // ---------------------------------------------------------------------------
-template <class R>
-size_t step_smem_bytes(int tj) {
-  switch (tj) {
-    case 4: return SmemPlan<R, 4>::total;
-    case 8: return SmemPlan<R, 8>::total;
-    case 16: return SmemPlan<R, 16>::total;
-    default: return 0;
-  }
-}
-
 template <class S, int TJ>
 static cudaError_t configure_tj() {
   return cudaFuncSetAttribute(fdtd_step_kernel<S, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)SmemPlan<typename S::R, TJ>::total);
+                              (int)SmemPlan<S, TJ>::bytes(TAB_ROWS_MAX));
 }
 
 template <class S>
@@ -645,7 +643,7 @@ static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_face
   dim3 block(TK, TJ);
   // fused: face points handled by extra blocks of the same launch
   dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + TK * TJ - 1) / (TK * TJ)));
-  fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<typename S::R, TJ>::total, st>>>(a);
+  fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<S, TJ>::bytes(a.nmat), st>>>(a);
   if (separate_faces && nfaces > 0) fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
@@ -688,7 +686,7 @@ __global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ 
     const int tt = *sa.step_base + ba.step_off;
     if (tt < sa.step_end) {
       const Roles<R> r = roles<S>(sa, tt);
-      tile_block<S, TJ>(sa, base, r, (R)__ldg(sa.src + tt), tt, tid, w.y, &ba.inst[w.x].tm_u, &ba.inst[w.x].tm_mat);
+      tile_block<S, TJ>(sa, base, r, (R)__ldg(sa.src + tt), tt, tid, w.y, ba.inst + w.x);
     }
     __syncthreads();  // sa and item are rewritten by the next iteration
   }
@@ -726,7 +724,7 @@ __global__ void batch_advance_kernel(const __grid_constant__ BatchArgs<R> ba, in
 template <class S, int TJ>
 static cudaError_t batch_launch_tj(const BatchArgs<typename S::R>& ba, int grid_tiles, int grid_faces,
                                    cudaStream_t st) {
-  batch_step_kernel<S, TJ><<<grid_tiles, dim3(TK, TJ), SmemPlan<typename S::R, TJ>::total, st>>>(ba);
+  batch_step_kernel<S, TJ><<<grid_tiles, dim3(TK, TJ), SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS), st>>>(ba);
   batch_face_kernel<S><<<grid_faces, 256, 0, st>>>(ba);
   return cudaGetLastError();
 }
@@ -743,7 +741,7 @@ cudaError_t batch_step(const BatchArgs<typename S::R>& ba, int tj, int grid_tile
 
 template <class S, int TJ>
 static cudaError_t batch_configure_tj(int* blocks_per_sm) {
-  const int smem = (int)SmemPlan<typename S::R, TJ>::total;
+  const int smem = (int)SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS);
   cudaError_t e = cudaFuncSetAttribute(batch_step_kernel<S, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_step_kernel<S, TJ>, TK * TJ, smem);

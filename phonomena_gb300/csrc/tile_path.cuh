@@ -1,7 +1,8 @@
 // Tile path of the fused step kernel (included by fdtd_step.cu).
 //
 // A block owns a (TJ x 32) tile of the (y, z) plane and marches along x over
-// planes [ib, ie).  Planes of u (3 components, 1-node halo) and material ids
+// planes [ib, ie).  Planes of u (3 components, 1-node halo), material ids and
+// the pointwise state of the own points (u_old, or v and the Kahan terms)
 // arrive by TMA in a 4-slot ring.  Every smem access uses offsets fixed per
 // thread (own position Lu / Lm, neighbours at constant distance), the range
 // predicates of the reference's slices are split into per-thread (j, k) and
@@ -16,10 +17,9 @@
 template <class S, int TJ>
 __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, unsigned char* base,
                                            const Roles<typename S::R>& r, const typename S::R s, const int tt,
-                                           const int tid, const int b, const CUtensorMap* tm_u,
-                                           const CUtensorMap* tm_mat) {
+                                           const int tid, const int b, const StepArgs<typename S::R>* maps) {
   using R = typename S::R;
-  using P = SmemPlan<R, TJ>;
+  using P = SmemPlan<S, TJ>;
   using TF = TileFetch<R, TJ>;
   constexpr int NT = TK * TJ;
   constexpr int W = P::W, PL = P::PL;
@@ -29,6 +29,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   uint64_t* bars = reinterpret_cast<uint64_t*>(base);
   R* stab = reinterpret_cast<R*>(base + P::off_tab);
   R* uring = reinterpret_cast<R*>(base + P::off_u);
+  R* pwring = reinterpret_cast<R*>(base + P::off_pw);
   uint8_t* mring = reinterpret_cast<uint8_t*>(base + P::off_m);
   R* sT2 = reinterpret_cast<R*>(base + P::off_t);
   R* sT3 = sT2 + PL;
@@ -53,6 +54,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   const int L = (ty + 1) * W + tx + 1;    // own entry of the stress planes
   const int Lu = (ty + 1) * KW + tx + KB;  // own entry of a u component tile
   const int Lm = (ty + 1) * MKW + tx + MKOFF;
+  const int Lp = ty * TK + tx;             // own entry of a pointwise component tile
 
   // the whole material table (nmat <= 256 rows) is staged in shared memory
   for (int q = tid; q < a.nmat * 16; q += NT) stab[q] = __ldg(a.tab + q);
@@ -86,12 +88,20 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   const bool rigid = a.bc == 1;
 
   // -------- TMA ring --------
+  // pointwise state is read for the planes whose points this block updates
+  const int pw_buf = (S::kahan ? r.rcur : r.rold) * 3;
   auto issue = [&](int p) {  // plane p into its ring slot (one thread)
     const int q = p - ibase, sl = q & (NSLOT - 1);
-    mbar_expect_tx(&bars[sl], P::tx_bytes);
-    // padded coordinates: k + KOFF, j + 1, i + 1; the tiles start at k0-KB, j0-1
-    tma_load_4d(uring + sl * SU, tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
-    tma_load_3d(mring + sl * SM, tm_mat, k0, j0, p + 1, &bars[sl]);
+    const bool pw = p >= ib && p < ie;
+    mbar_expect_tx(&bars[sl], P::tx_bytes + (pw ? P::pw_bytes : 0u));
+    // padded coordinates: k + KOFF, j + 1, i + 1; the u tiles start at k0-KB, j0-1
+    tma_load_4d(uring + sl * SU, &maps->tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
+    tma_load_3d(mring + sl * SM, &maps->tm_mat, k0, j0, p + 1, &bars[sl]);
+    if (pw) {
+      R* d = pwring + sl * P::PWS;
+      tma_load_4d(d, &maps->tm_pw0, k0 + Lay<R>::KOFF, j0 + 1, p + 1, pw_buf, &bars[sl]);
+      if constexpr (S::kahan) tma_load_4d(d + 3 * P::PWC, &maps->tm_pw1, k0 + Lay<R>::KOFF, j0 + 1, p + 1, pw_buf, &bars[sl]);
+    }
   };
   bool ok = true;
   auto wait_plane = [&](int p) {
@@ -100,6 +110,11 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   };
   auto uslot = [&](int p) { return uring + ((p - ibase) & (NSLOT - 1)) * SU; };
   auto mslot = [&](int p) { return mring + ((p - ibase) & (NSLOT - 1)) * SM; };
+  // pointwise state of component c at the own point of plane p
+  auto pw_at = [&](int p, int c) {
+    const R* t = pwring + ((p - ibase) & (NSLOT - 1)) * P::PWS + c * P::PWC + Lp;
+    return Pw<R>{t[0], S::kahan ? t[3 * P::PWC] : R(0)};
+  };
 
   if (tid == 0) {
     for (int q = 0; q < NSLOT; q++) mbar_init(&bars[q], 1);
@@ -188,15 +203,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   }
   R t1m = 0, uxm = 0, uxm_up = 0;
 
-  // pointwise state prefetch, one plane ahead: ux at plane i-1, uy/uz at plane i
-  // (V0 points only: u_new there depends on u_old / v / c of the same point)
   const long long off_j = g.o0 + (long long)j * g.sy + k;
-  auto want_y = [&](int i) { return active && i < ie && !face_y && i >= 1 && i <= nx - 2; };
-  auto want_z = [&](int i) { return active && i < ie && !face_z && i >= 1 && i <= nx - 2 && j_n; };
-  auto want_x = [&](int i) { return active && i > ib && i - 1 < ie && !face_x && i - 1 != nx - 2 && j_n; };
-  Pw<R> pwx{0, 0}, pwy{0, 0}, pwz{0, 0};
-  if (want_y(ib)) pwy = load_pw<S>(r, 1, off_j + (long long)ib * g.sx);
-  if (want_z(ib)) pwz = load_pw<S>(r, 2, off_j + (long long)ib * g.sx);
 
   // x spacings of plane p: fdx[p] (T5, T6 at p; ux at p+1) and sdx[p-1]
   // (T1..T3 at p; uy, uz at p), read one plane ahead so that their latency
@@ -208,10 +215,6 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   for (int i = ib; i <= ie; i++) {
     const long long off_i = off_j + (long long)i * g.sx;  // (i, j, k)
     const R fx_next = fx_at(i + 1), sx_next = sx_at(i + 1);
-    Pw<R> nx_{0, 0}, ny_{0, 0}, nz_{0, 0};
-    if (want_x(i + 1)) nx_ = load_pw<S>(r, 0, off_i);
-    if (want_y(i + 1)) ny_ = load_pw<S>(r, 1, off_i + g.sx);
-    if (want_z(i + 1)) nz_ = load_pw<S>(r, 2, off_i + g.sx);
     // per-plane (uniform) predicates and spacings
     const bool i_n = i >= 1 && i <= nx - 2;  // T1..T4
     const bool i_s = i <= nx - 2;            // T5, T6 (i >= 0 here)
@@ -297,6 +300,9 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     }
     const R uxc = U0[XO + Lu], uyc = U0[YO + Lu], uzc = U0[ZO + Lu];
     const R uxc_up = U0[XO + Lu + 1];  // ux(i, j, k+1): z = N face input of the next plane's ux
+    // ux is updated one plane behind: its pointwise state is taken from the
+    // slot of plane i-1 before that slot is refilled
+    const Pw<R> pwx = pw_at(i - 1, 0);
     __syncthreads();
     // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
     if (tid == 0 && i - 1 + NSLOT <= plast) {
@@ -314,7 +320,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             const R dv = S::div3(S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
                                  S::sub(t4c, sT4[L - 1]), uy_c);
             R vn, cn;
-            val = update_value<S>(uyc, pwy, dv, row, vn, cn);
+            val = update_value<S>(uyc, pw_at(i, 1), dv, row, vn, cn);
             store_point<S>(r, 1, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 1, off_i);
@@ -332,7 +338,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             const R dv = S::div3(S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
                                  S::sub(sT3[L + 1], t3c), uz_c);
             R vn, cn;
-            val = update_value<S>(uzc, pwz, dv, row, vn, cn);
+            val = update_value<S>(uzc, pw_at(i, 2), dv, row, vn, cn);
             store_point<S>(r, 2, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 2, off_i);
@@ -371,9 +377,6 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     sx_cur = sx_next;
     uxm = uxc;
     uxm_up = uxc_up;
-    pwx = nx_;
-    pwy = ny_;
-    pwz = nz_;
   }
   if (!ok) {
     // a pipeline wait ran out: flag it and drain the copies this block issued
