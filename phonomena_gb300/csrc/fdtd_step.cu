@@ -266,26 +266,23 @@ __device__ __forceinline__ typename S::R div_z(const StepArgs<typename S::R>& a,
 // (no pointer arrays, which would live in local memory)
 template <class R>
 struct Roles {
-  R* ubase;
-  R* vbase;
-  R* cbase;
+  // component-0 array of each role (component c at + c * fs), set once per
+  // launch: an access is the point's offset added to a block-uniform base
+  R *u_cur, *u_old, *u_out, *v_in, *v_out, *c_in, *c_out;
   long long fs;
   int rold, rcur, rout;  // buffer indices: u at tt-1 (F64), tt, tt+1
-  __device__ __forceinline__ const R* cur(int c) const { return ubase + (rcur * 3 + c) * fs; }
-  __device__ __forceinline__ const R* old(int c) const { return ubase + (rold * 3 + c) * fs; }
-  __device__ __forceinline__ R* out(int c) const { return ubase + (rout * 3 + c) * fs; }
-  __device__ __forceinline__ const R* vin(int c) const { return vbase + (rcur * 3 + c) * fs; }
-  __device__ __forceinline__ const R* cin(int c) const { return cbase + (rcur * 3 + c) * fs; }
-  __device__ __forceinline__ R* vout(int c) const { return vbase + (rout * 3 + c) * fs; }
-  __device__ __forceinline__ R* cout(int c) const { return cbase + (rout * 3 + c) * fs; }
+  __device__ __forceinline__ const R* cur(int c) const { return u_cur + c * fs; }
+  __device__ __forceinline__ const R* old(int c) const { return u_old + c * fs; }
+  __device__ __forceinline__ R* out(int c) const { return u_out + c * fs; }
+  __device__ __forceinline__ const R* vin(int c) const { return v_in + c * fs; }
+  __device__ __forceinline__ const R* cin(int c) const { return c_in + c * fs; }
+  __device__ __forceinline__ R* vout(int c) const { return v_out + c * fs; }
+  __device__ __forceinline__ R* cout(int c) const { return c_out + c * fs; }
 };
 
 template <class S>
 __device__ __forceinline__ Roles<typename S::R> roles(const StepArgs<typename S::R>& a, int tt) {
   Roles<typename S::R> r;
-  r.ubase = a.ubase;
-  r.vbase = a.vbase;
-  r.cbase = a.cbase;
   r.fs = a.g.fstride;
   if (!S::kahan) {
     r.rold = tt % 3;
@@ -296,6 +293,14 @@ __device__ __forceinline__ Roles<typename S::R> roles(const StepArgs<typename S:
     r.rout = r.rcur ^ 1;
     r.rold = r.rcur;
   }
+  const long long f3 = 3 * r.fs;
+  r.u_cur = a.ubase + r.rcur * f3;
+  r.u_old = a.ubase + r.rold * f3;
+  r.u_out = a.ubase + r.rout * f3;
+  r.v_in = a.vbase + r.rcur * f3;
+  r.v_out = a.vbase + r.rout * f3;
+  r.c_in = a.cbase + r.rcur * f3;
+  r.c_out = a.cbase + r.rout * f3;
   return r;
 }
 
@@ -592,9 +597,18 @@ struct SmemPlan {
 // ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
-// FP32: 32 resident warps per SM (64 registers, no spills); FP64: 16 warps
+// Resident blocks per SM the register allocation is made for (measured on
+// GB300 for the 256x256x128 crystal and the 64-crystal batch).  FP32 step
+// kernel: 6 blocks of 128 threads (85 registers), 4 of 256 (64), 2 of 512
+// (64); the persistent batch kernel holds more state and gets twice the
+// registers at TJ 8 / 16.  FP64: 16 warps per SM.
+template <class R, int TJ, bool BATCH = false>
+struct MinBlocks {
+  static constexpr int value = sizeof(R) == 8 ? (TJ < 16 ? 16 / TJ : 1)
+                               : (TJ == 4 ? 6 : (TJ == 8 ? (BATCH ? 2 : 4) : (BATCH ? 1 : 2)));
+};
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : (TJ < 16 ? 16 / TJ : 1)))
+__global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ>::value)
     fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -662,7 +676,7 @@ cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int separate_f
 // batched instances: persistent tile kernel + face kernel + counter update
 // ---------------------------------------------------------------------------
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK* TJ, (sizeof(typename S::R) == 4 ? 32 / TJ : (TJ < 16 ? 16 / TJ : 1)))
+__global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ, true>::value)
     batch_step_kernel(const __grid_constant__ BatchArgs<typename S::R> ba) {
   using R = typename S::R;
   extern __shared__ __align__(128) unsigned char smem_raw[];

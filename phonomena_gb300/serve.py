@@ -53,6 +53,7 @@ class Result:
     admitted: float
     finished: float
     surface: np.ndarray          # (steps // record_every, nx, ny) uz at z = 0
+    error: str = None            # set when the run stopped early (non-finite values)
 
     @property
     def latency(self):
@@ -158,7 +159,25 @@ class GpuBackend:
         self.batch.step(nsteps)
 
     def sync(self):
-        self.batch.sync()
+        """Wait for the batch; returns the slots whose simulation reported
+        non-finite values (its own error flag; the others are unaffected)."""
+        from ._lib import PhonoError
+
+        try:
+            self.batch.sync()
+            return []
+        except PhonoError as e:
+            if e.code != -5:
+                raise
+        bad = []
+        for slot, sim in self.batch.members.items():
+            try:
+                sim.sync()
+            except PhonoError as e:
+                if e.code != -5:
+                    raise
+                bad.append(slot)
+        return bad
 
     def remaining(self, slot):
         return self.batch.remaining(slot)
@@ -314,12 +333,16 @@ class Server:
             self.stats.chunks += 1
             finished = [s for s in active if self.backend.remaining(s) == 0]
             if finished:
-                self.backend.sync()
+                failed = set(self.backend.sync())
                 t = self.now()
-                for s in finished:
+                # a simulation that produced non-finite values ends now, with
+                # the records it has; the rest of the mix goes on
+                for s in sorted(failed | set(finished)):
                     req, sim, admitted, need = active.pop(s)
+                    ran = req.steps - self.backend.remaining(s)
                     surf = self.backend.finish(s, sim)  # memory stays held by the pool
-                    res = Result(req.rid, int(np.prod(req.spec.nodes)), req.steps, req.arrival, admitted, t, surf)
+                    res = Result(req.rid, int(np.prod(req.spec.nodes)), ran, req.arrival, admitted, t, surf,
+                                 error="non-finite values" if s in failed else None)
                     self.stats.results.append(res)
                     if self.on_result is not None:
                         self.on_result(res)
@@ -360,7 +383,7 @@ def summarize(results, makespan=None):
             "p95_s": float(np.percentile(lat, 95)), "p99_s": float(np.percentile(lat, 99)),
             "mean_wait_s": float(np.mean([r.wait for r in results])),
             "gcell_updates_per_s": work / makespan / 1e9, "makespan_s": makespan,
-            "cell_updates": int(work)}
+            "cell_updates": int(work), "failed": sum(1 for r in results if r.error)}
 
 
 def mean_work(n=4000, seed=0, **kw):

@@ -22,6 +22,7 @@ class FakeBackend:
         self.peak = 0
         self.max_active = 0
         self.steps_log = []
+        self.diverging = set()  # requests whose simulation "overflows" after 20 steps
 
     def clock(self):
         return self.t
@@ -67,14 +68,15 @@ class FakeBackend:
             a[2] += adv
 
     def sync(self):
-        pass
+        bad = [s for s, a in self.active.items() if a[0].req.rid in self.diverging and a[2] >= 20]
+        return bad
 
     def remaining(self, slot):
         return self.active[slot][1]
 
     def finish(self, slot, sim):
         p, rem, done = self.active.pop(slot)
-        assert rem == 0 and done == p.req.steps
+        assert (rem == 0 and done == p.req.steps) or p.req.rid in self.diverging
         k = self.key(p)
         self.pool[k] = self.pool.get(k, 0) + 1
         # the "surface" of a request depends on its own inputs only
@@ -96,8 +98,9 @@ def stream(n, seed=0, rate=50.0):
     return out
 
 
-def run(reqs, budget, capacity, chunk=60):
+def run(reqs, budget, capacity, chunk=60, diverging=()):
     be = FakeBackend(budget, capacity)
+    be.diverging = set(diverging)
     srv = serve.Server(be, budget_bytes=budget, capacity=capacity, chunk=chunk, prepare_fn=fake_prepare,
                        clock=be.clock, workers=2)
     res = srv.run(reqs, realtime=False)
@@ -168,3 +171,14 @@ def test_poisson_stream_distribution():
     for r in reqs:
         if r.spec.cells != (512, 512, 128):
             assert r.spec.cells[0] in (64, 96, 128, 160, 192) and r.spec.cells[2] in (32, 48, 64, 96)
+
+
+def test_failed_request_ends_alone():
+    """A simulation with non-finite values ends early with an error; the others finish normally."""
+    reqs = stream(12, seed=5)
+    be, srv, res = run(reqs, budget=10 ** 12, capacity=4, diverging={3})
+    by = {r.rid: r for r in res}
+    assert sorted(by) == list(range(12))
+    assert by[3].error and by[3].steps < reqs[3].steps
+    assert all(r.error is None and r.steps == reqs[r.rid].steps for r in res if r.rid != 3)
+    assert serve.summarize(res)["failed"] == 1
