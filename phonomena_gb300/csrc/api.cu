@@ -473,6 +473,10 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->g.sx = (long long)(ny + 2) * pz;
   h->g.o0 = h->g.sx + h->g.sy + koff;
   h->field_elems = (size_t)(nx + 2) * h->g.sx;
+  if (h->field_elems >= (1ull << 32)) {  // the tile pass addresses an array with 32-bit offsets
+    delete h;
+    return fail(PHONO_ERR_ARG, "grid too large: one padded array exceeds 2^32 elements");
+  }
   h->g.fstride = (long long)h->field_elems;
   const long long mpz = mat_row(nz);
   h->g.msy = mpz;

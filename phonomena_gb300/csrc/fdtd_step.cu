@@ -343,8 +343,10 @@ __device__ __forceinline__ typename S::R update_value(typename S::R u, Pw<typena
   }
 }
 
-template <class S>
-__device__ __forceinline__ void store_point(const Roles<typename S::R>& r, int c, long long off, typename S::R un,
+// OFF: element offset inside one array; the tile path passes a 32-bit
+// unsigned offset (one multiply-add per address), the face path 64-bit
+template <class S, class OFF>
+__device__ __forceinline__ void store_point(const Roles<typename S::R>& r, int c, OFF off, typename S::R un,
                                             typename S::R vn, typename S::R cn) {
   r.out(c)[off] = un;
   if constexpr (S::kahan) {
@@ -354,8 +356,8 @@ __device__ __forceinline__ void store_point(const Roles<typename S::R>& r, int c
 }
 
 // a point the reference does not write this step keeps its state; returns u
-template <class S>
-__device__ __forceinline__ typename S::R store_stale(const Roles<typename S::R>& r, int c, long long off) {
+template <class S, class OFF>
+__device__ __forceinline__ typename S::R store_stale(const Roles<typename S::R>& r, int c, OFF off) {
   const typename S::R u = __ldg(r.cur(c) + off);
   r.out(c)[off] = u;
   if constexpr (S::kahan) {

@@ -110,11 +110,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   };
   auto uslot = [&](int p) { return uring + ((p - ibase) & (NSLOT - 1)) * SU; };
   auto mslot = [&](int p) { return mring + ((p - ibase) & (NSLOT - 1)) * SM; };
-  // pointwise state of component c at the own point of plane p
-  auto pw_at = [&](int p, int c) {
-    const R* t = pwring + ((p - ibase) & (NSLOT - 1)) * P::PWS + c * P::PWC + Lp;
-    return Pw<R>{t[0], S::kahan ? t[3 * P::PWC] : R(0)};
-  };
+
 
   if (tid == 0) {
     for (int q = 0; q < NSLOT; q++) mbar_init(&bars[q], 1);
@@ -189,6 +185,92 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     return S::ts(c, d1, kzero ? a.sp.fdx0 : fy, d2, kzero ? a.sp.fdz0 : fx);
   };
 
+  // Halo stresses the neighbours need: T2 row j0+TJ, T6 / T4 row j0-1, T3
+  // column k0+TK, T4 / T5 column k0-1, one per thread (the first three warps
+  // take one row kind each, the next the columns; 3*TK + 3*TJ <= TK*TJ).
+  // All but the plane index is fixed for the tile, so the kind, the smem
+  // indices (absolute, tile origin at KW+KB / MKW+MKOFF), the range test and
+  // the spacings (with the z = 0 row's substitutions, base_solver.py:420-433)
+  // are set up once here.
+  static_assert(3 * TK + 3 * TJ <= NT, "one halo task per thread");
+  int hk = -1, h_u = 0, h_m = 0, h_dst = 0, h_which = 1;
+  bool h_ok = false, h_z0 = false;
+  R h_a = R(1), h_b = R(1);
+  {
+    const int u0 = KW + KB, m0 = MKW + MKOFF;  // tile origin (jl = 0, kl = 0)
+    const int qq = tid;
+    if (qq < TK) {  // T2 at (j0+TJ, k0+qq)
+      const int jj = j0 + TJ, kk = k0 + qq;
+      hk = 0;
+      h_which = 1;
+      h_u = u0 + TJ * KW + qq;
+      h_m = m0 + TJ * MKW + qq;
+      h_dst = (TJ + 1) * W + qq + 1;
+      h_ok = jj >= 1 && jj <= ny - 2 && kk <= nz - 2;
+      h_z0 = kk == 0;
+      if (h_ok) {
+        h_a = h_z0 ? a.sp.sdy0 : __ldg(a.sp.sdy + jj - 1);
+        h_b = h_z0 ? a.sp.sdz0 : __ldg(a.sp.sdz + kk - 1);
+      }
+    } else if (qq < 2 * TK) {  // T6 at (j0-1, k0+q)
+      const int q = qq - TK, jj = j0 - 1, kk = k0 + q;
+      hk = 1;
+      h_u = u0 - KW + q;
+      h_m = m0 - MKW + q + MKW;
+      h_dst = q + 1;
+      h_ok = jj >= 0 && jj <= ny - 2 && kk <= nz - 2;
+      h_z0 = kk == 0;
+      if (h_ok) h_a = h_z0 ? a.sp.fdx0 : __ldg(a.sp.fdy + jj);
+    } else if (qq < 3 * TK) {  // T4 at (j0-1, k0+q)
+      const int q = qq - 2 * TK, jj = j0 - 1, kk = k0 + q;
+      hk = 2;
+      h_u = u0 - KW + q;
+      h_m = m0 - MKW + q + MKW + (kk == 0 ? 0 : 1);
+      h_dst = q + 1;
+      h_ok = jj >= 0 && jj <= ny - 2 && kk <= nz - 2;
+      if (h_ok) {
+        h_a = kk == 0 ? a.sp.fdy0 : __ldg(a.sp.fdz + kk);
+        h_b = kk == 0 ? a.sp.fdz0 : __ldg(a.sp.fdy + jj);
+      }
+    } else if (qq < 3 * TK + 3 * TJ) {
+      const int w = qq - 3 * TK;
+      const int which = w / TJ, jl = w - which * TJ;
+      const int jj = j0 + jl;
+      if (which == 0) {  // T3 at (j0+jl, k0+TK): kk >= 32, never the z = 0 row
+        const int kk = k0 + TK;
+        hk = 0;
+        h_which = 2;
+        h_u = u0 + jl * KW + TK;
+        h_m = m0 + jl * MKW + TK;
+        h_dst = (jl + 1) * W + TK + 1;
+        h_ok = jj >= 1 && jj <= ny - 2 && kk <= nz - 2;
+        if (h_ok) {
+          h_a = __ldg(a.sp.sdy + jj - 1);
+          h_b = __ldg(a.sp.sdz + kk - 1);
+        }
+      } else if (which == 1) {  // T4 at (j0+jl, k0-1): kk >= 31 when valid
+        const int kk = k0 - 1;
+        hk = 2;
+        h_u = u0 + jl * KW - 1;
+        h_m = m0 + jl * MKW - 1 + MKW + 1;
+        h_dst = (jl + 1) * W;
+        h_ok = jj <= ny - 2 && kk >= 0 && kk <= nz - 2;
+        if (h_ok) {
+          h_a = __ldg(a.sp.fdz + kk);
+          h_b = __ldg(a.sp.fdy + jj);
+        }
+      } else {  // T5 at (j0+jl, k0-1)
+        const int kk = k0 - 1;
+        hk = 3;
+        h_u = u0 + jl * KW - 1;
+        h_m = m0 + jl * MKW - 1 + 1;
+        h_dst = (jl + 1) * W;
+        h_ok = jj >= 1 && jj <= ny - 2 && kk >= 0 && kk <= nz - 2;
+        if (h_ok) h_a = __ldg(a.sp.fdz + kk);
+      }
+    }
+  }
+
   // prologue stresses: own T5, T6 at plane ib-1
   R t5m, t6m;
   {
@@ -203,7 +285,18 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   }
   R t1m = 0, uxm = 0, uxm_up = 0;
 
-  const long long off_j = g.o0 + (long long)j * g.sy + k;
+  // which component updates this thread owns (loop-invariant), and the
+  // surface record this step writes (none: nullptr)
+  const bool own_y = active && !face_y, own_z = active && !face_z, own_x = active && !face_x;
+  R* rec = nullptr;
+  if (kz && a.record_every > 0 && (tt + 1) % a.record_every == 0) {
+    const int slot = (tt + 1) / a.record_every - 1 - a.rec_base;
+    if (slot >= 0 && slot < a.nrec_cap) rec = a.surf + ((long long)slot * nx) * ny + j;
+  }
+
+  // element offsets inside one array fit in 32 bits (checked at handle creation)
+  const unsigned off_j = (unsigned)(g.o0 + (long long)j * g.sy + k);
+  const unsigned sxu = (unsigned)g.sx;
 
   // x spacings of plane p: fdx[p] (T5, T6 at p; ux at p+1) and sdx[p-1]
   // (T1..T3 at p; uy, uz at p), read one plane ahead so that their latency
@@ -213,7 +306,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   R fx_prev = fx_at(ib - 1), fx_cur = fx_at(ib), sx_cur = sx_at(ib);
 
   for (int i = ib; i <= ie; i++) {
-    const long long off_i = off_j + (long long)i * g.sx;  // (i, j, k)
+    const unsigned off_i = off_j + (unsigned)i * sxu;  // (i, j, k)
     const R fx_next = fx_at(i + 1), sx_next = sx_at(i + 1);
     // per-plane (uniform) predicates and spacings
     const bool i_n = i >= 1 && i <= nx - 2;  // T1..T4
@@ -243,76 +336,63 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     sT4[L] = t4c;
     sT5[p * PL + L] = t5c;
     sT6[p * PL + L] = t6c;
-    // halo stresses the neighbours need: T2 row j0+TJ, T6/T4 row j0-1,
-    // T3 column k0+TK, T4/T5 column k0-1.  Offsets are relative to the thread
-    // at (ty, tx) = (0, 0) of the tile, so Lu/Lm must be subtracted back.
-    // Task qq runs on thread qq: each of the first three warps computes one
-    // row kind, the fourth the three column kinds.
-    for (int qq = tid; qq < 3 * TK + 3 * TJ; qq += NT) {
-      const int du0 = -Lu + KW + KB, dm0 = -Lm + MKW + MKOFF;  // shift to tile origin (jl=0, kl=0)
-      if (qq < TK) {  // T2 at (j0+TJ, k0+qq)
-        const int jj = j0 + TJ, kk = k0 + qq;
-        R v = R(0);
-        if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2) {
-          const bool z0 = kk == 0;
-          v = T1one(Um, U0, M0, du0 + TJ * KW + qq, dm0 + TJ * MKW + qq, 1, z0 ? a.sp.sdx0 : sdx_im,
-                    z0 ? a.sp.sdy0 : __ldg(a.sp.sdy + jj - 1), z0 ? a.sp.sdz0 : __ldg(a.sp.sdz + kk - 1));
+    // this thread's halo stress of plane i (set up before the loop)
+    if (hk >= 0) {
+      R v = R(0);
+      if (hk == 0) {  // T2 row above / T3 column right: one row of the T1-T3 formula
+        if (i_n && h_ok) {
+          const R* c = tab + 16 * M0[h_m] + 3 * h_which;
+          const R d1 = S::sub(U0[XO + h_u], Um[XO + h_u]);
+          const R d2 = S::sub(U0[YO + h_u], U0[YO + h_u - KW]);
+          const R d3 = S::sub(U0[ZO + h_u], U0[ZO + h_u - 1]);
+          v = S::tn1(c, d1, d2, d3, h_z0 ? a.sp.sdx0 : sdx_im, h_a, h_b);
         }
-        sT2[(TJ + 1) * W + qq + 1] = v;
-      } else if (qq < 2 * TK) {  // T6 at (j0-1, k0+q)
-        const int q = qq - TK, jj = j0 - 1, kk = k0 + q;
-        R v = R(0);
-        if (i_s && jj >= 0 && jj <= ny - 2 && kk <= nz - 2)
-          v = T6f(U0, Up, Mp, du0 - KW + q, dm0 - MKW + q, kk == 0, __ldg(a.sp.fdy + jj), fdx_i);
-        sT6[p * PL + q + 1] = v;
-      } else if (qq < 3 * TK) {  // T4 at (j0-1, k0+q)
-        const int q = qq - 2 * TK, jj = j0 - 1, kk = k0 + q;
-        R v = R(0);
-        if (i_n && jj >= 0 && jj <= ny - 2 && kk <= nz - 2)
-          v = T4f(U0, M0, du0 - KW + q, dm0 - MKW + q, kk == 0, __ldg(a.sp.fdz + kk), __ldg(a.sp.fdy + jj));
-        sT4[q + 1] = v;
-      } else {
-        const int w = qq - 3 * TK;
-        const int which = w / TJ, jl = w - which * TJ;
-        const int jj = j0 + jl;
-        if (which == 0) {  // T3 at (j0+jl, k0+TK)
-          const int kk = k0 + TK;
-          R v = R(0);
-          if (i_n && jj >= 1 && jj <= ny - 2 && kk <= nz - 2)  // kk >= 32: never the z = 0 row
-            v = T1one(Um, U0, M0, du0 + jl * KW + TK, dm0 + jl * MKW + TK, 2, sdx_im, __ldg(a.sp.sdy + jj - 1),
-                      __ldg(a.sp.sdz + kk - 1));
-          sT3[(jl + 1) * W + TK + 1] = v;
-        } else if (which == 1) {  // T4 at (j0+jl, k0-1)
-          const int kk = k0 - 1;
-          R v = R(0);
-          if (i_n && jj <= ny - 2 && kk >= 0 && kk <= nz - 2)
-            v = T4f(U0, M0, du0 + jl * KW - 1, dm0 + jl * MKW - 1, kk == 0, __ldg(a.sp.fdz + kk),
-                    __ldg(a.sp.fdy + jj));
-          sT4[(jl + 1) * W] = v;
-        } else {  // T5 at (j0+jl, k0-1)
-          const int kk = k0 - 1;
-          R v = R(0);
-          if (i_s && jj >= 1 && jj <= ny - 2 && kk >= 0 && kk <= nz - 2)
-            v = T5f(U0, Up, Mp, du0 + jl * KW - 1, dm0 + jl * MKW - 1, kk == 0, __ldg(a.sp.fdz + kk), fdx_i);
-          sT5[p * PL + (jl + 1) * W] = v;
+        (h_which == 1 ? sT2 : sT3)[h_dst] = v;
+      } else if (hk == 1) {  // T6 row below
+        if (i_s && h_ok) {
+          const R c = tab[16 * Mp[h_m] + 11];
+          const R d1 = S::sub(U0[XO + h_u + KW], U0[XO + h_u]);
+          const R d2 = S::sub(Up[YO + h_u], U0[YO + h_u]);
+          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
         }
+        sT6[p * PL + h_dst] = v;
+      } else if (hk == 2) {  // T4 row below / column left
+        if (i_n && h_ok) {
+          const R c = tab[16 * M0[h_m] + 9];
+          const R d1 = S::sub(U0[YO + h_u + 1], U0[YO + h_u]);
+          const R d2 = S::sub(U0[ZO + h_u + KW], U0[ZO + h_u]);
+          v = S::ts(c, d1, h_a, d2, h_b);
+        }
+        sT4[h_dst] = v;
+      } else {  // T5 column left
+        if (i_s && h_ok) {
+          const R c = tab[16 * Mp[h_m] + 10];
+          const R d1 = S::sub(U0[XO + h_u + 1], U0[XO + h_u]);
+          const R d2 = S::sub(Up[ZO + h_u], U0[ZO + h_u]);
+          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
+        }
+        sT5[p * PL + h_dst] = v;
       }
     }
     const R uxc = U0[XO + Lu], uyc = U0[YO + Lu], uzc = U0[ZO + Lu];
     const R uxc_up = U0[XO + Lu + 1];  // ux(i, j, k+1): z = N face input of the next plane's ux
     // ux is updated one plane behind: its pointwise state is taken from the
     // slot of plane i-1 before that slot is refilled
-    const Pw<R> pwx = pw_at(i - 1, 0);
+    const R* PWm = pwring + ((i - 1 - ibase) & (NSLOT - 1)) * P::PWS + Lp;  // pointwise, plane i-1
+    const Pw<R> pwx{PWm[0], S::kahan ? PWm[3 * P::PWC] : R(0)};
     __syncthreads();
     // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
     if (tid == 0 && i - 1 + NSLOT <= plast) {
       issue(i - 1 + NSLOT);
       issued = i - 1 + NSLOT;
     }
-    if (active) {
-      if (i < ie) {
+    const R* PW0 = pwring + ((i - ibase) & (NSLOT - 1)) * P::PWS + Lp;  // pointwise, plane i
+    const bool plane_yz = i < ie;                            // uy, uz of plane i belong to this segment
+    const bool plane_x = i > ib && i - 1 != nx - 2;         // ux of plane i-1 (not the x = N face)
+    {
+      if (plane_yz) {
         // uy_new(i, j, k)   (base_solver.py:449-455, 503-509)
-        if (!face_y) {
+        if (own_y) {
           R val;
           if (i_n) {
             // at k = 0 the T4(k-1) halo entry is 0, so T4 - 0 is the z = 0 row's "T4 - 0"
@@ -320,7 +400,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             const R dv = S::div3(S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
                                  S::sub(t4c, sT4[L - 1]), uy_c);
             R vn, cn;
-            val = update_value<S>(uyc, pw_at(i, 1), dv, row, vn, cn);
+            val = update_value<S>(uyc, Pw<R>{PW0[P::PWC], S::kahan ? PW0[4 * P::PWC] : R(0)}, dv, row, vn, cn);
             store_point<S>(r, 1, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 1, off_i);
@@ -329,7 +409,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             store_point<S>(r, 1, off_i + 1, rigid ? R(0) : S::abc(a.abc[6], val, U0[YO + Lu + 1], uyc), R(0), R(0));
         }
         // uz_new(i, j, k)   (base_solver.py:457-463, 511-516)
-        if (!face_z) {
+        if (own_z) {
           R val;
           if (i_n && j_n) {
             // z = 0 row: density at z index 0 (base_solver.py:513); T3(k) = 0 there,
@@ -338,19 +418,22 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             const R dv = S::div3(S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
                                  S::sub(sT3[L + 1], t3c), uz_c);
             R vn, cn;
-            val = update_value<S>(uzc, pw_at(i, 2), dv, row, vn, cn);
+            val = update_value<S>(uzc, Pw<R>{PW0[2 * P::PWC], S::kahan ? PW0[5 * P::PWC] : R(0)}, dv, row, vn, cn);
             store_point<S>(r, 2, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 2, off_i);
           }
-          if (kz) record(a, tt, i, j, val);
+          if (kz) {  // surface uz (base_solver.py:114-116) and the non-finite guard
+            if (rec) rec[(long long)i * ny] = val;
+            if (!isfinite(val)) atomicOr(a.err, 1);
+          }
           if (zface_z)  // uz on z = N from its inner neighbour (base_solver.py:554)
             store_point<S>(r, 2, off_i + 1, rigid ? R(0) : S::abc(a.abc[7], val, U0[ZO + Lu + 1], uzc), R(0), R(0));
         }
       }
-      if (i > ib && !face_x && i - 1 != nx - 2) {
+      if (plane_x && own_x) {
         // ux_new(i-1, j, k)   (base_solver.py:441-447, 495-501)
-        const long long off = off_i - g.sx;
+        const unsigned off = off_i - sxu;
         R val;
         if (j_n) {
           const int pm = p ^ 1;
