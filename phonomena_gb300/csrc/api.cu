@@ -219,6 +219,7 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.vbase = (R*)h->vbase;
   a.cbase = (R*)h->cbase;
   for (int q = 0; q < 8; q++) a.abc[q] = (R)h->abc[q];
+  a.dt = (R)h->d.dt;
   a.surf = (R*)h->surf;
   a.record_every = h->d.record_every;
   a.rec_base = 0;

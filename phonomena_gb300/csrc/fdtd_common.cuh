@@ -90,6 +90,7 @@ struct StepArgs {
   R* vbase;      // F32K velocity arrays (2 buffers x 3), same layout
   R* cbase;      // F32K Kahan compensation arrays
   R abc[8];      // clx[-1] ctx[-1] cty[0] cly[0] cty[-1] cly[-1] ctz[-1] clz[-1]
+  R dt;          // time step (the table's column 14, the same for every material)
   R* surf;       // surface records: [slot][nx][ny]
   int record_every;
   int rec_base;  // record slot of the first record kept in surf

@@ -323,24 +323,31 @@ __device__ __forceinline__ Pw<typename S::R> load_pw(const Roles<typename S::R>&
   return p;
 }
 
-// new state of one V0 point: F64 leapfrog / F32K Kahan velocity update
+// new state of one V0 point: F64 leapfrog / F32K Kahan velocity update.
+// q = the table's column 12 at the point (dt^2/P or dt/P), dt = column 14.
 template <class S>
 __device__ __forceinline__ typename S::R update_value(typename S::R u, Pw<typename S::R> pw, typename S::R dv,
-                                                      const typename S::R* row, typename S::R& vn,
+                                                      typename S::R q, typename S::R dt, typename S::R& vn,
                                                       typename S::R& cn) {
   using R = typename S::R;
   if constexpr (!S::kahan) {
     // (2u - u_old) + (dt^2/P) * div   (base_solver.py:441-443)
     vn = cn = 0;
-    return __dadd_rn(__dsub_rn(__dmul_rn(2.0, u), pw.p0), __dmul_rn(row[12], dv));
+    return __dadd_rn(__dsub_rn(__dmul_rn(2.0, u), pw.p0), __dmul_rn(q, dv));
   } else {
-    R v2 = S::fma(row[12], dv, pw.p0);  // row[12] = dt / P
-    R y = S::fma(row[14], v2, -pw.p1);   // row[14] = dt
+    R v2 = S::fma(q, dv, pw.p0);   // v + (dt/P) div
+    R y = S::fma(dt, v2, -pw.p1);  // dt v - c
     R t = S::add(u, y);
     cn = S::sub(S::sub(t, u), y);
     vn = v2;
     return t;
   }
+}
+template <class S>
+__device__ __forceinline__ typename S::R update_value(typename S::R u, Pw<typename S::R> pw, typename S::R dv,
+                                                      const typename S::R* row, typename S::R& vn,
+                                                      typename S::R& cn) {
+  return update_value<S>(u, pw, dv, row[12], row[14], vn, cn);
 }
 
 // OFF: element offset inside one array; the tile path passes a 32-bit

@@ -146,30 +146,6 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   // spacings and material index it uses: its "uz - 0" is the interior
   // difference against the zero padding at k = -1.  So each stress is one
   // evaluation on selected operands, never two evaluations and a select.
-  auto T123 = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, R sa, R sb, R sd, R& T1, R& T2,
-                  R& T3) {
-    const R* c = tab + 16 * M0[Lm + dm];
-    const R d1 = S::sub(U0[XO + Lu + du], Um[XO + Lu + du]);
-    const R d2 = S::sub(U0[YO + Lu + du], U0[YO + Lu + du - KW]);
-    const R d3 = S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
-    T1 = S::tn1(c, d1, d2, d3, sa, sb, sd);
-    T2 = S::tn1(c + 3, d1, d2, d3, sa, sb, sd);
-    T3 = S::tn1(c + 6, d1, d2, d3, sa, sb, sd);
-  };
-  auto T1one = [&](const R* Um, const R* U0, const uint8_t* M0, int du, int dm, int which, R sa, R sb, R sd) {
-    const R* c = tab + 16 * M0[Lm + dm] + 3 * which;
-    const R d1 = S::sub(U0[XO + Lu + du], Um[XO + Lu + du]);
-    const R d2 = S::sub(U0[YO + Lu + du], U0[YO + Lu + du - KW]);
-    const R d3 = S::sub(U0[ZO + Lu + du], U0[ZO + Lu + du - 1]);
-    return S::tn1(c, d1, d2, d3, sa, sb, sd);
-  };
-  // T4 (base_solver.py:353-358, 420-423)
-  auto T4f = [&](const R* U0, const uint8_t* M0, int du, int dm, bool kzero, R fz, R fy) {
-    const R c = tab[16 * M0[Lm + dm + MKW + (kzero ? 0 : 1)] + 9];
-    const R d1 = S::sub(U0[YO + Lu + du + 1], U0[YO + Lu + du]);
-    const R d2 = S::sub(U0[ZO + Lu + du + KW], U0[ZO + Lu + du]);
-    return S::ts(c, d1, kzero ? a.sp.fdy0 : fz, d2, kzero ? a.sp.fdz0 : fy);
-  };
   // T5 (base_solver.py:360-365, 425-428)
   auto T5f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fz, R fx) {
     const R c = tab[16 * Mp[Lm + dm + (kzero ? 0 : 1)] + 10];
@@ -283,7 +259,14 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     t5m = (i_s && j_n && k_in) ? T5f(U0, Up, Mp, 0, 0, kz, fdz_k, fx) : R(0);
     t6m = (i_s && j_s && k_in) ? T6f(U0, Up, Mp, 0, 0, kz, fdy_j, fx) : R(0);
   }
-  R t1m = 0, uxm = 0, uxm_up = 0;
+  R t1m = 0, uxm_up = 0;
+  // values carried from plane to plane instead of re-read from the ring:
+  // ux at i-1 (T1's x difference, ux's own value one plane behind), uy and
+  // uz at i (read as plane i+1 values one iteration earlier), and the
+  // material ids of plane i the next plane's loads already fetched
+  R uxm = uslot(ib - 1)[XO + Lu];
+  R uyc_n = uslot(ib)[YO + Lu], uzc_n = uslot(ib)[ZO + Lu];
+  int id_c = mslot(ib)[Lm], id_z = mslot(ib)[Lm + 1], id_y = mslot(ib)[Lm + MKW];
 
   // which component updates this thread owns (loop-invariant), and the
   // surface record this step writes (none: nullptr)
@@ -320,17 +303,51 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     const R* Up = uslot(i + 1);
     const uint8_t* M0 = mslot(i);
     const uint8_t* Mp = mslot(i + 1);
-    // own stresses at plane i
-    R t1c, t2c, t3c;
+    // own stresses at plane i, each read of the ring once
+    const R uxc = U0[XO + Lu], uyc = uyc_n, uzc = uzc_n;
+    uyc_n = Up[YO + Lu];
+    uzc_n = Up[ZO + Lu];
+    const R uxc_up = U0[XO + Lu + 1];  // ux(i, j, k+1): T5, and the z = N face input of the next plane's ux
+    const int idp_c = Mp[Lm], idp_z = Mp[Lm + 1], idp_y = Mp[Lm + MKW];
+    R t1c = R(0), t2c = R(0), t3c = R(0);
     if (i_n && j_n && k_in) {
-      T123(Um, U0, M0, 0, 0, kz ? a.sp.sdx0 : sdx_im, t123_b, t123_d, t1c, t2c, t3c);
-      if (kz) t3c = R(0);  // T3[1:-1,1:-1,0] = 0 (base_solver.py:418)
-    } else {
-      t1c = t2c = t3c = R(0);
+      // T1..T3 (base_solver.py:329-351, 408-418): material of the own node
+      const R* row = tab + 16 * id_c;
+      R cc[9];
+      if constexpr (sizeof(R) == 4) {
+        const float4 q0 = *reinterpret_cast<const float4*>(row), q1 = *reinterpret_cast<const float4*>(row + 4);
+        cc[0] = q0.x, cc[1] = q0.y, cc[2] = q0.z, cc[3] = q0.w, cc[4] = q1.x, cc[5] = q1.y, cc[6] = q1.z, cc[7] = q1.w;
+        cc[8] = row[8];
+      } else {
+        for (int q = 0; q < 9; q++) cc[q] = row[q];
+      }
+      const R d1 = S::sub(uxc, uxm);
+      const R d2 = S::sub(uyc, U0[YO + Lu - KW]);
+      const R d3 = S::sub(uzc, U0[ZO + Lu - 1]);
+      const R sa = kz ? a.sp.sdx0 : sdx_im;
+      t1c = S::tn1(cc, d1, d2, d3, sa, t123_b, t123_d);
+      t2c = S::tn1(cc + 3, d1, d2, d3, sa, t123_b, t123_d);
+      if (!kz) t3c = S::tn1(cc + 6, d1, d2, d3, sa, t123_b, t123_d);  // T3[1:-1,1:-1,0] = 0 (:418)
     }
-    const R t4c = (i_n && j_s && k_in) ? T4f(U0, M0, 0, 0, kz, fdz_k, fdy_j) : R(0);
-    const R t5c = (i_s && j_n && k_in) ? T5f(U0, Up, Mp, 0, 0, kz, fdz_k, fdx_i) : R(0);
-    const R t6c = (i_s && j_s && k_in) ? T6f(U0, Up, Mp, 0, 0, kz, fdy_j, fdx_i) : R(0);
+    R t4c = R(0), t5c = R(0), t6c = R(0);
+    if (i_n && j_s && k_in) {  // T4 (base_solver.py:353-358, 420-423)
+      const R c = tab[16 * (kz ? id_y : (int)M0[Lm + MKW + 1]) + 9];
+      const R d1 = S::sub(U0[YO + Lu + 1], uyc);
+      const R d2 = S::sub(U0[ZO + Lu + KW], uzc);
+      t4c = S::ts(c, d1, kz ? a.sp.fdy0 : fdz_k, d2, kz ? a.sp.fdz0 : fdy_j);
+    }
+    if (i_s && j_n && k_in) {  // T5 (base_solver.py:360-365, 425-428)
+      const R c = tab[16 * (kz ? idp_c : idp_z) + 10];
+      const R d1 = S::sub(uxc_up, uxc);
+      const R d2 = S::sub(uzc_n, uzc);
+      t5c = S::ts(c, d1, kz ? a.sp.fdx0 : fdz_k, d2, kz ? a.sp.fdz0 : fdx_i);
+    }
+    if (i_s && j_s && k_in) {  // T6 (base_solver.py:367-372, 430-433)
+      const R c = tab[16 * idp_y + 11];
+      const R d1 = S::sub(U0[XO + Lu + KW], uxc);
+      const R d2 = S::sub(uyc_n, uyc);
+      t6c = S::ts(c, d1, kz ? a.sp.fdx0 : fdy_j, d2, kz ? a.sp.fdz0 : fdx_i);
+    }
     sT2[L] = t2c;
     sT3[L] = t3c;
     sT4[L] = t4c;
@@ -374,8 +391,6 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
         sT5[p * PL + h_dst] = v;
       }
     }
-    const R uxc = U0[XO + Lu], uyc = U0[YO + Lu], uzc = U0[ZO + Lu];
-    const R uxc_up = U0[XO + Lu + 1];  // ux(i, j, k+1): z = N face input of the next plane's ux
     // ux is updated one plane behind: its pointwise state is taken from the
     // slot of plane i-1 before that slot is refilled
     const R* PWm = pwring + ((i - 1 - ibase) & (NSLOT - 1)) * P::PWS + Lp;  // pointwise, plane i-1
@@ -396,11 +411,12 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           R val;
           if (i_n) {
             // at k = 0 the T4(k-1) halo entry is 0, so T4 - 0 is the z = 0 row's "T4 - 0"
-            const R* row = tab + 16 * M0[Lm + MKW];
+            const R* row = tab + 16 * id_y;
             const R dv = S::div3(S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
                                  S::sub(t4c, sT4[L - 1]), uy_c);
             R vn, cn;
-            val = update_value<S>(uyc, Pw<R>{PW0[P::PWC], S::kahan ? PW0[4 * P::PWC] : R(0)}, dv, row, vn, cn);
+            val = update_value<S>(uyc, Pw<R>{PW0[P::PWC], S::kahan ? PW0[4 * P::PWC] : R(0)}, dv, row[12], a.dt, vn,
+                                  cn);
             store_point<S>(r, 1, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 1, off_i);
@@ -414,11 +430,12 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           if (i_n && j_n) {
             // z = 0 row: density at z index 0 (base_solver.py:513); T3(k) = 0 there,
             // and the reference precedence (:516) adds T3[..,1] with factor 1
-            const R* row = tab + 16 * M0[Lm + (kz ? 0 : 1)];
+            const R* row = tab + 16 * (kz ? id_c : id_z);
             const R dv = S::div3(S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
                                  S::sub(sT3[L + 1], t3c), uz_c);
             R vn, cn;
-            val = update_value<S>(uzc, Pw<R>{PW0[2 * P::PWC], S::kahan ? PW0[5 * P::PWC] : R(0)}, dv, row, vn, cn);
+            val = update_value<S>(uzc, Pw<R>{PW0[2 * P::PWC], S::kahan ? PW0[5 * P::PWC] : R(0)}, dv, row[12], a.dt,
+                                  vn, cn);
             store_point<S>(r, 2, off_i, val, vn, cn);
           } else {
             val = store_stale<S>(r, 2, off_i);
@@ -437,13 +454,13 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
         R val;
         if (j_n) {
           const int pm = p ^ 1;
-          const R* row = tab + 16 * M0[Lm];  // P[(i-1)+1, j, k]
+          const R* row = tab + 16 * id_c;  // P[(i-1)+1, j, k]
           // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
           const R dv = S::div3(S::sub(t1c, t1m), kz ? a.sp.fdx0 : fdx_im,
                                S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]), ux_b,
                                S::sub(sT5[pm * PL + L], sT5[pm * PL + L - 1]), ux_c);
           R vn, cn;
-          val = update_value<S>(uxm, pwx, dv, row, vn, cn);
+          val = update_value<S>(uxm, pwx, dv, row[12], a.dt, vn, cn);
           store_point<S>(r, 0, off, val, vn, cn);
         } else {
           val = store_stale<S>(r, 0, off);
@@ -460,6 +477,9 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     sx_cur = sx_next;
     uxm = uxc;
     uxm_up = uxc_up;
+    id_c = idp_c;
+    id_z = idp_z;
+    id_y = idp_y;
   }
   if (!ok) {
     // a pipeline wait ran out: flag it and drain the copies this block issued
