@@ -601,23 +601,44 @@ struct SmemPlan {
   static_assert((PWC * sizeof(R)) % 128 == 0 && (TF::SU * sizeof(R)) % 128 == 0, "ring tiles must stay 128-byte aligned");
 };
 
+// Rows of one z column a tile-pass thread owns: two for the FP32 velocity
+// form at tile heights 8 and 16 (the per-plane work shared by two nodes; 128
+// or 256 threads a block), one otherwise.
+template <class S, int TJ>
+struct RowsPerThread {
+  static constexpr int value = (S::kahan && sizeof(typename S::R) == 4 && TJ >= 8) ? 2 : 1;
+};
+
 #include "tile_path.cuh"
+#include "tile_rows.cuh"
+
+// the tile pass of one block: one row per thread or RowsPerThread rows
+template <class S, int TJ>
+__device__ __forceinline__ bool run_tile(const StepArgs<typename S::R>& a, unsigned char* base,
+                                         const Roles<typename S::R>& r, const typename S::R s, const int tt,
+                                         const int tid, const int b, const StepArgs<typename S::R>* maps) {
+  if constexpr (RowsPerThread<S, TJ>::value == 1)
+    return tile_block<S, TJ>(a, base, r, s, tt, tid, b, maps);
+  else
+    return tile_block_rows<S, TJ>(a, base, r, s, tt, tid, b, maps);
+}
 
 // ---------------------------------------------------------------------------
 // the step kernel
 // ---------------------------------------------------------------------------
 // Resident blocks per SM the register allocation is made for (measured on
-// GB300 for the 256x256x128 crystal and the 64-crystal batch).  FP32 step
-// kernel: 6 blocks of 128 threads (85 registers), 4 of 256 (64), 2 of 512
-// (64); the persistent batch kernel holds more state and gets twice the
-// registers at TJ 8 / 16.  FP64: 16 warps per SM.
+// GB300 for the 256x256x128 crystal and the 64-crystal batch).  FP32: tile
+// height 4, 6 blocks of 128 threads (up to 85 registers); heights 8 and 16
+// (two rows a thread), 4 blocks of 128 or 2 of 256 threads (up to 128
+// registers).  FP64: 16 warps per SM.
 template <class R, int TJ, bool BATCH = false>
 struct MinBlocks {
-  static constexpr int value = sizeof(R) == 8 ? (TJ < 16 ? 16 / TJ : 1)
-                               : (TJ == 4 ? 6 : (TJ == 8 ? (BATCH ? 2 : 4) : (BATCH ? 1 : 2)));
+  static constexpr int value = sizeof(R) == 8 ? (TJ < 16 ? 16 / TJ : 1) : (TJ == 4 ? 6 : (TJ == 8 ? 4 : 2));
 };
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ>::value)
+__host__ __device__ constexpr int step_threads() { return TK * TJ / RowsPerThread<S, TJ>::value; }
+template <class S, int TJ>
+__global__ void __launch_bounds__(step_threads<S, TJ>(), MinBlocks<typename S::R, TJ>::value)
     fdtd_step_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -633,12 +654,12 @@ __global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ>::value)
 
   if ((int)blockIdx.x >= a.n_tile_blocks) {
     // ---------------- face blocks (fused launch) ----------------
-    face_point<S>(a, r, s, tt, ((int)blockIdx.x - a.n_tile_blocks) * (TK * TJ) + tid, false);
+    face_point<S>(a, r, s, tt, ((int)blockIdx.x - a.n_tile_blocks) * step_threads<S, TJ>() + tid, false);
     return;
   }
 
   // ---------------- tile blocks ----------------
-  tile_block<S, TJ>(a, base, r, s, tt, tid, blockIdx.x, &a);
+  run_tile<S, TJ>(a, base, r, s, tt, tid, blockIdx.x, &a);
 }
 
 // ---------------------------------------------------------------------------
@@ -663,9 +684,10 @@ cudaError_t configure_step(int tj) {
 template <class S, int TJ>
 static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_faces, cudaStream_t st) {
   const int nfaces = a.faces.off[12];
-  dim3 block(TK, TJ);
+  constexpr int NT = step_threads<S, TJ>();
+  dim3 block(TK, NT / TK);
   // fused: face points handled by extra blocks of the same launch
-  dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + TK * TJ - 1) / (TK * TJ)));
+  dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + NT - 1) / NT));
   fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<S, TJ>::bytes(a.nmat), st>>>(a);
   if (separate_faces && nfaces > 0) fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
   return cudaGetLastError();
@@ -685,7 +707,7 @@ cudaError_t launch_step(const StepArgs<typename S::R>& a, int tj, int separate_f
 // batched instances: persistent tile kernel + face kernel + counter update
 // ---------------------------------------------------------------------------
 template <class S, int TJ>
-__global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ, true>::value)
+__global__ void __launch_bounds__(step_threads<S, TJ>(), MinBlocks<typename S::R, TJ, true>::value)
     batch_step_kernel(const __grid_constant__ BatchArgs<typename S::R> ba) {
   using R = typename S::R;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -704,12 +726,12 @@ __global__ void __launch_bounds__(TK* TJ, MinBlocks<typename S::R, TJ, true>::va
     const int2 w = ba.items[it];
     const int4* src4 = reinterpret_cast<const int4*>(ba.inst + w.x);
     int4* dst4 = reinterpret_cast<int4*>(&sa);
-    for (int q = tid; q < (int)(sizeof(StepArgs<R>) / 16); q += TK * TJ) dst4[q] = src4[q];
+    for (int q = tid; q < (int)(sizeof(StepArgs<R>) / 16); q += step_threads<S, TJ>()) dst4[q] = src4[q];
     __syncthreads();
     const int tt = *sa.step_base + ba.step_off;
     if (tt < sa.step_end) {
       const Roles<R> r = roles<S>(sa, tt);
-      tile_block<S, TJ>(sa, base, r, (R)__ldg(sa.src + tt), tt, tid, w.y, ba.inst + w.x);
+      run_tile<S, TJ>(sa, base, r, (R)__ldg(sa.src + tt), tt, tid, w.y, ba.inst + w.x);
     }
     __syncthreads();  // sa and item are rewritten by the next iteration
   }
@@ -747,7 +769,8 @@ __global__ void batch_advance_kernel(const __grid_constant__ BatchArgs<R> ba, in
 template <class S, int TJ>
 static cudaError_t batch_launch_tj(const BatchArgs<typename S::R>& ba, int grid_tiles, int grid_faces,
                                    cudaStream_t st) {
-  batch_step_kernel<S, TJ><<<grid_tiles, dim3(TK, TJ), SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS), st>>>(ba);
+  batch_step_kernel<S, TJ>
+      <<<grid_tiles, dim3(TK, step_threads<S, TJ>() / TK), SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS), st>>>(ba);
   batch_face_kernel<S><<<grid_faces, 256, 0, st>>>(ba);
   return cudaGetLastError();
 }
@@ -767,7 +790,8 @@ static cudaError_t batch_configure_tj(int* blocks_per_sm) {
   const int smem = (int)SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS);
   cudaError_t e = cudaFuncSetAttribute(batch_step_kernel<S, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_step_kernel<S, TJ>, TK * TJ, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, batch_step_kernel<S, TJ>, step_threads<S, TJ>(),
+                                                       smem);
 }
 
 template <class S>
