@@ -392,7 +392,7 @@ def bench_serve(args, rank, world, local, torch, dist):
     from phonomena_gb300 import serve
 
     budget = args.budget_gb * 1e9
-    gcell32, gcell64 = 35.0, 1.5  # batched throughputs used to set the default rates
+    gcell32, gcell64 = 45.0, 1.6  # batched throughputs used to set the default rates
     rate32 = args.rate or serve.rate_for_load(gcell32, 0.7)
     rate64 = rate32 * gcell64 / gcell32
 
@@ -552,11 +552,9 @@ def main():
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        from phonomena_gb300 import replicas
+
+        return replicas.aggregate(x, 0.0, dist)[0]
 
     # ---- FP32 Kahan: device-resident throughput ----
     sim = DeviceSimulation(sp, m.ids, m.table, m.dt, precision="f32k", **kw("f32k"))

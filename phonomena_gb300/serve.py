@@ -94,7 +94,7 @@ class GpuBackend:
     ``max_steps`` steps so that requests of any length share a key.
     """
 
-    def __init__(self, precision="f32k", capacity=128, tile_j=8, x_segment=0, max_steps=3000):
+    def __init__(self, precision="f32k", capacity=128, tile_j=16, x_segment=0, max_steps=3000):
         from .batch import Batch
 
         self.precision = precision
