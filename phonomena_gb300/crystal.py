@@ -78,6 +78,18 @@ def material_ids(spec: CrystalSpec):
         kind = np.full((npx, npy), 2, np.uint8)
     else:
         kind = np.where(rng.uniform(size=(npx, npy)) < spec.tungsten_frac, 2, 1).astype(np.uint8)
+    # Lattice cells whose hole would cover a node of the two layers at an
+    # absorbing face (x = N, y = 0, y = N) stay solid host.  The reference's
+    # first-order absorbing faces (simulation/base_solver.py:519-554) use the
+    # host's wave speeds and go unstable next to a void or an inclusion: a
+    # 128x128x48 crystal with a = 12 grew to max|u| = 1.2e4 after 1500 steps,
+    # 4.8 with the cut cells left solid.  The benchmark crystals with whole
+    # cells and r <= 0.4a clear the faces and are unchanged by this rule.
+    ccx = (np.arange(npx) + 0.5) * a
+    ccy = (np.arange(npy) + 0.5) * a
+    reach = (ccx[:, None] + radii > spec.cells[0] - 1) | (ccy[None, :] + radii > spec.cells[1] - 1) | \
+            (ccy[None, :] - radii < 1)
+    kind = np.where(reach, 0, kind).astype(np.uint8)
     x = np.arange(nx, dtype=np.float64)
     y = np.arange(ny, dtype=np.float64)
     px = np.minimum((x // a).astype(int), npx - 1)

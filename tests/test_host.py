@@ -157,3 +157,13 @@ def test_footprint_is_the_padded_layout():
     assert footprint((nx, ny, nz), "f64", steps, 0) < footprint((nx, ny, nz), "f64v", steps, 0)
     with pytest.raises(Exception):
         footprint((2, 5, 5), "f32k", 10, 1)
+
+
+def test_crystal_holes_clear_the_absorbing_faces():
+    """No void or inclusion node in the two node layers next to x = N, y = 0, y = N."""
+    from phonomena_gb300 import crystal
+
+    for spec in crystal.config4_specs(n=24, seed=3, steps=10):
+        ids = crystal.material_ids(spec)
+        assert not ids[-2:].any() and not ids[:, :2].any() and not ids[:, -2:].any(), spec.cells
+        assert ids.any()  # the lattice is still there
