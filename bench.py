@@ -9,7 +9,7 @@ Gcell-updates/s = mesh nodes x time steps / s (nodes = (cells+1)^3, the
 reference's "points", tests/test_speed.py:52).
 
 value: device time (CUDA events on the solver's stream) with all state
-resident in HBM; the state (612 MB) is larger than L2.  e2e: wall time
+resident in HBM; the state (770 MB) is larger than L2.  e2e: wall time
 through the public API with pinned host buffers: per step the material ids
 and source go host->device and the surface records and final uz come back.
 
@@ -673,7 +673,7 @@ def main():
             "config": {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({nodes} nodes), {S} time steps "
                                    "per bench step from the zero state, FP32 velocity form with Kahan-compensated u, "
                                    "corrected z=0 row, absorbing walls, uz surface every 10 steps",
-                       "nodes": nodes, "fdtd_steps": S, "l2": "inputs larger than L2 (state 612 MB)",
+                       "nodes": nodes, "fdtd_steps": S, "l2": "inputs larger than L2 (state 770 MB)",
                        "parallelism": f"replicas x{world}"},
             "fp64": {"value": round(value64, 4), "unit": "Gcell-updates/s", "fdtd_steps": S,
                      "ms": round(ms64, 3), "speedup_f32k_over_f64": round(value / value64, 3),

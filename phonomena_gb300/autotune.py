@@ -17,9 +17,10 @@ kernel's work does not depend on the values), so tuning never touches the
 caller's state.  Results are cached per (scheme, shapes, device) in a JSON
 file next to the built library, so a mesh or a mix is tuned once per machine.
 
-tile_j sets the block (32 x tile_j threads, shared memory per block); the
-x segment sets how many x planes a block marches and thereby the number of
-blocks (several waves of the 152 SMs vs. the re-read of three halo planes per
+tile_j sets the block (a 32 x tile_j tile: 32 x tile_j threads at height 4,
+two rows a thread at 8 and 16 in FP32; shared memory per block); the x
+segment sets how many x planes a block marches and thereby the number of
+blocks (several waves of the 152 SMs vs. the re-read of two halo planes per
 segment).
 """
 from __future__ import annotations
@@ -33,7 +34,7 @@ import numpy as np
 
 CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 TILE_J = (4, 8, 16)
-X_SEGMENTS = (16, 24, 32, 40, 48, 64)
+X_SEGMENTS = (12, 16, 20, 24, 28, 32, 40, 48, 64)
 DEFAULT = (8, 32)
 _HOST_ROW = np.array([[224e9, 64e9, 64e9, 64e9, 224e9, 64e9, 64e9, 64e9, 224e9, 80e9, 80e9, 80e9, 2330.0]])
 
