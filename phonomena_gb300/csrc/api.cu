@@ -267,7 +267,7 @@ static size_t handle_bytes(int nx, int ny, int nz, int precision, int max_steps,
   const size_t fb = field_elems * es * 3 * nbuf;
   size_t total = r(fb) * (precision == PHONO_F64 ? 1 : 3);
   const int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
-  for (int a = 0; a < 6; a++) total += r((size_t)lens[a] * es) + r((size_t)lens[a] * 8);
+  for (int a = 0; a < 6; a++) total += r((size_t)(lens[a] + 3) * es) + r((size_t)lens[a] * 8);
   total += r((size_t)(nx + 2) * (ny + 2) * mat_row(nz));
   total += r((size_t)256 * 16 * es) + r((size_t)256 * PHONO_TABLE_COLS * 8);
   const int cap = max_steps > 0 ? max_steps : 1;
@@ -533,22 +533,25 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   // spacings
   const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
   int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
+  // device copies carry one value 1 before and two after the array, so the
+  // tile pass reads the x spacings of its planes -1..nx without range tests
+  // (the padding only reaches values whose results are discarded)
   for (int a = 0; a < 6; a++) {
     h->h_sp0[a] = arrs[a][0];
     h->sp_host[a].assign(arrs[a], arrs[a] + lens[a]);
-    TRY(dalloc(h, &h->sp[a], (size_t)lens[a] * h->es));
+    void* spb = nullptr;
+    TRY(dalloc(h, &spb, (size_t)(lens[a] + 3) * h->es));
+    h->sp[a] = (char*)spb + h->es;
     TRY(dalloc(h, (void**)&h->sp64[a], (size_t)lens[a] * 8));
     TRYC(cudaMemcpy(h->sp64[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
-    if (f64) {
-      TRYC(cudaMemcpy(h->sp[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
-    } else if (h->es == 8) {  // F64V: reciprocals in double
-      std::vector<double> r(lens[a]);
-      for (int q = 0; q < lens[a]; q++) r[q] = 1.0 / arrs[a][q];
-      TRYC(cudaMemcpy(h->sp[a], r.data(), (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    if (h->es == 8) {  // F64: raw spacings; F64V: reciprocals in double
+      std::vector<double> r(lens[a] + 3, 1.0);
+      for (int q = 0; q < lens[a]; q++) r[q + 1] = f64 ? arrs[a][q] : 1.0 / arrs[a][q];
+      TRYC(cudaMemcpy(spb, r.data(), r.size() * 8, cudaMemcpyHostToDevice));
     } else {
-      std::vector<float> r(lens[a]);
-      for (int q = 0; q < lens[a]; q++) r[q] = (float)(1.0 / arrs[a][q]);
-      TRYC(cudaMemcpy(h->sp[a], r.data(), (size_t)lens[a] * 4, cudaMemcpyHostToDevice));
+      std::vector<float> r(lens[a] + 3, 1.0f);
+      for (int q = 0; q < lens[a]; q++) r[q + 1] = (float)(1.0 / arrs[a][q]);
+      TRYC(cudaMemcpy(spb, r.data(), r.size() * 4, cudaMemcpyHostToDevice));
     }
   }
   // materials: padded id layout and the 16-entry device rows (capacity 256 ids)

@@ -284,8 +284,9 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   // x spacings of plane p: fdx[p] (T5, T6 at p; ux at p+1) and sdx[p-1]
   // (T1..T3 at p; uy, uz at p), read one plane ahead so that their latency
   // is not on the path of the stress evaluation
-  auto fx_at = [&](int p) { return p >= 0 && p <= nx - 2 ? __ldg(a.sp.fdx + p) : R(1); };
-  auto sx_at = [&](int p) { return p >= 1 && p <= nx - 2 ? __ldg(a.sp.sdx + p - 1) : R(1); };
+  // (the spacing arrays are padded: p runs over -1..nx)
+  auto fx_at = [&](int p) { return __ldg(a.sp.fdx + p); };
+  auto sx_at = [&](int p) { return __ldg(a.sp.sdx + p - 1); };
   R fx_prev = fx_at(ib - 1), fx_cur = fx_at(ib), sx_cur = sx_at(ib);
 
   for (int i = ib; i <= ie; i++) {

@@ -149,7 +149,7 @@ def test_footprint_is_the_padded_layout():
     fe = (nx + 2) * (ny + 2) * row
     want = 3 * r(fe * 4 * 3 * 2)  # u (2 buffers), v, c: three components each
     for n in (nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2):
-        want += r(n * 4) + r(n * 8)
+        want += r((n + 3) * 4) + r(n * 8)  # device spacings carry 1 + 2 pad values
     want += r((nx + 2) * (ny + 2) * (-(-(8 + nz + 1) // 16) * 16))  # ids
     want += r(256 * 16 * 4) + r(256 * 13 * 8) + r(steps * 8) + r(steps // rec * nx * ny * 4)
     want += r(8) + r(16 * 1024) + r(16)
