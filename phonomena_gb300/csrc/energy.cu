@@ -4,7 +4,7 @@
 // writes, E_str = 1/2 sum T . e over the stress points the reference computes
 // (normal stresses at nodes, shears at edges; simulation/base_solver.py:323-433)
 // with unit weights.  v is the half-step velocity: (u - u_old)/dt for the
-// leapfrog state, the stored v for the velocity form.  Used only to judge the
+// leapfrog state, the stored v for the velocity form.  Used only to measure the
 // error of the FP32 path against the FP64 path; the reference has no energy.
 //
 // Pass 1 writes one partial pair per block into a scratch array; pass 2 sums
