@@ -128,6 +128,26 @@ int phono_reset(phono_handle *h);
  * (material.py:55-63) on the device. */
 int phono_set_materials(phono_handle *h, const uint8_t *mat, const double *table, int nmat);
 
+/* Material ids of a phononic crystal built on the device: a square lattice
+ * (pitch `pitch` cells, ncx x ncy cells, cell (p, q) covering nodes
+ * [p*pitch, (p+1)*pitch) in x and y, the last cell also the rest) of vertical
+ * cylindrical holes centred in their cells, from z = 0 down through node
+ * `depth`.  A node is inside the hole of its cell when its squared distance
+ * from the centre is below the squared radius (FP64).  Inside: the cell's id;
+ * elsewhere: `host`.  The table as in phono_set_materials.  Replaces the
+ * reference's per-node fill of the inclusion nodes (material.py:59-63,
+ * grid.py:158-175) with one kernel.  No reference counterpart as a call. */
+typedef struct phono_lattice {
+  int pitch;             /* lattice pitch in cells */
+  int ncx, ncy;          /* lattice cells along x and y */
+  const double *radius;  /* ncx*ncy hole radii in cells, x slowest */
+  const uint8_t *kind;   /* ncx*ncy material id inside each hole */
+  int depth;             /* holes fill z = 0..depth (nodes) */
+  int host;              /* material id outside the holes */
+} phono_lattice;
+
+int phono_set_lattice(phono_handle *h, const phono_lattice *lat, const double *table, int nmat);
+
 /* The handle's cudaStream_t (as void*), for callers that record their own
  * CUDA events around phono_step. */
 void *phono_stream(phono_handle *h);
@@ -147,6 +167,17 @@ int phono_read_surface(phono_handle *h, int first, int count, void *host_out);
  * the reference leaves in g.ux, g.uy, g.uz after run. */
 int phono_download(phono_handle *h, int field, void *host, size_t bytes);
 int phono_upload(phono_handle *h, int field, const void *host, size_t bytes);
+
+/* Checkpoint / resume (no reference counterpart; for preempting and
+ * restarting long runs).  A checkpoint is the state fields of the scheme
+ * (F64: UX..UZ and UX_OLD..UZ_OLD; F32K / F64V: UX..UZ, VX..VZ, CX..CZ), the
+ * step count and the surface records so far.  To resume into a handle made
+ * with the same description and source: phono_set_steps_done first (it
+ * selects the buffers the fields belong to), then phono_upload of each field
+ * and phono_upload_surface of the records; the run then continues bit for
+ * bit as if it had not stopped. */
+int phono_set_steps_done(phono_handle *h, int steps);
+int phono_upload_surface(phono_handle *h, int first, int count, const void *host_in);
 
 /* Element size in bytes of the handle's fields (8 or 4). */
 int phono_elem_size(const phono_handle *h);

@@ -27,7 +27,8 @@ EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
            "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
            "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
-           "phono_batch_destroy", "phono_set_tiling", "phono_footprint",
+           "phono_batch_destroy", "phono_set_tiling", "phono_footprint", "phono_set_steps_done",
+           "phono_upload_surface", "phono_set_lattice",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
 
@@ -60,6 +61,14 @@ class PhonoEnergyDense(ctypes.Structure):
         ("fdx", ctypes.c_void_p), ("fdy", ctypes.c_void_p), ("fdz", ctypes.c_void_p),
         ("sdx", ctypes.c_void_p), ("sdy", ctypes.c_void_p), ("sdz", ctypes.c_void_p),
         ("dt", ctypes.c_double),
+    ]
+
+
+class PhonoLattice(ctypes.Structure):
+    """phono_lattice of include/phono.h: a lattice of cylindrical holes."""
+    _fields_ = [
+        ("pitch", ctypes.c_int), ("ncx", ctypes.c_int), ("ncy", ctypes.c_int),
+        ("radius", ctypes.c_void_p), ("kind", ctypes.c_void_p), ("depth", ctypes.c_int), ("host", ctypes.c_int),
     ]
 
 
@@ -102,6 +111,9 @@ def load(path: Path | None = None):
         "phono_batch_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_batch_destroy": (None, [vp]),
         "phono_set_tiling": (ci, [vp, ci, ci]),
+        "phono_set_steps_done": (ci, [vp, ci]),
+        "phono_upload_surface": (ci, [vp, ci, ci, vp]),
+        "phono_set_lattice": (ci, [vp, ctypes.POINTER(PhonoLattice), vp, ci]),
         "phono_footprint": (ci, [ci, ci, ci, ci, ci, ci, ctypes.POINTER(ctypes.c_size_t)]),
         "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_destroy": (None, [vp]),

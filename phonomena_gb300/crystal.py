@@ -66,10 +66,10 @@ class CrystalSpec:
         return nx * ny * nz
 
 
-def material_ids(spec: CrystalSpec):
-    """(nx, ny, nz) uint8 ids: 0 host, 1 void, 2 tungsten."""
+def lattice(spec: CrystalSpec):
+    """The crystal's hole lattice: pitch, per-cell radii (cells) and material
+    ids (0 host, 1 void, 2 tungsten), and the depth of the holes (nodes)."""
     rng = np.random.default_rng(spec.seed)
-    nx, ny, nz = spec.nodes
     a = spec.lattice
     npx, npy = -(-spec.cells[0] // a), -(-spec.cells[1] // a)
     lo, hi = spec.radius
@@ -90,6 +90,14 @@ def material_ids(spec: CrystalSpec):
     reach = (ccx[:, None] + radii > spec.cells[0] - 1) | (ccy[None, :] + radii > spec.cells[1] - 1) | \
             (ccy[None, :] - radii < 1)
     kind = np.where(reach, 0, kind).astype(np.uint8)
+    return {"pitch": a, "radius": radii, "kind": kind, "depth": spec.depth, "host": 0}
+
+
+def ids_from_lattice(nodes, lat):
+    """(nx, ny, nz) uint8 ids of a hole lattice (the host-side twin of phono_set_lattice)."""
+    nx, ny, nz = nodes
+    a, radii, kind = lat["pitch"], lat["radius"], lat["kind"]
+    npx, npy = radii.shape
     x = np.arange(nx, dtype=np.float64)
     y = np.arange(ny, dtype=np.float64)
     px = np.minimum((x // a).astype(int), npx - 1)
@@ -99,11 +107,16 @@ def material_ids(spec: CrystalSpec):
     d2 = (x - cx)[:, None] ** 2 + (y - cy)[None, :] ** 2
     r = radii[px[:, None], py[None, :]]
     inside = d2 < r * r
-    plane = np.where(inside, kind[px[:, None], py[None, :]], 0).astype(np.uint8)
-    ids = np.zeros((nx, ny, nz), np.uint8)
-    kmax = min(spec.depth, nz - 1)
+    plane = np.where(inside, kind[px[:, None], py[None, :]], lat["host"]).astype(np.uint8)
+    ids = np.full((nx, ny, nz), lat["host"], np.uint8)
+    kmax = min(lat["depth"], nz - 1)
     ids[:, :, : kmax + 1] = plane[:, :, None]
     return ids
+
+
+def material_ids(spec: CrystalSpec):
+    """(nx, ny, nz) uint8 ids: 0 host, 1 void, 2 tungsten."""
+    return ids_from_lattice(spec.nodes, lattice(spec))
 
 
 def build(spec: CrystalSpec):

@@ -21,6 +21,8 @@ cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, do
 cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st);
 cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, int n, cudaStream_t st);
 cudaError_t batch_configure_any(int precision, int tj, int* blocks_per_sm);
+cudaError_t launch_lattice_ids(uint8_t* mat, const Geo& g, int pitch, int ncx, int ncy, const double* radius,
+                               const uint8_t* kind, int depth, uint8_t host, cudaStream_t st);
 
 __global__ void advance_step_kernel(int* p, int n) { *p += n; }
 }  // namespace phono
@@ -145,6 +147,8 @@ static int check_materials(const phono_handle* h, const uint8_t* mat, const doub
 }
 
 // ids into the padded layout, 16-entry device rows, raw rows, ABC coefficients
+static int upload_table(phono_handle* h, const double* table, int nmat, int id000);
+
 static int upload_materials(phono_handle* h, const uint8_t* mat, const double* table, int nmat) {
   const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
   cudaMemcpy3DParms p{};
@@ -153,6 +157,12 @@ static int upload_materials(phono_handle* h, const uint8_t* mat, const double* t
   p.extent = make_cudaExtent(nz, ny, nx);
   p.kind = cudaMemcpyHostToDevice;
   CK(cudaMemcpy3DAsync(&p, h->stream));
+  return upload_table(h, table, nmat, mat[0]);
+}
+
+// the 16-entry device rows of the material table; id000 = the material at
+// node (0, 0, 0), whose wave speeds set the absorbing-face coefficients
+static int upload_table(phono_handle* h, const double* table, int nmat, int id000) {
   const double dt = h->d.dt;
   const double dt2 = dt * dt;
   if (h->es == 8) {
@@ -183,7 +193,7 @@ static int upload_materials(phono_handle* h, const uint8_t* mat, const double* t
   CK(cudaMemcpyAsync(h->tab13, table, (size_t)nmat * PHONO_TABLE_COLS * 8, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   h->nmat = nmat;
-  abc_coeffs(h, table + (size_t)mat[0] * PHONO_TABLE_COLS, h->abc);
+  abc_coeffs(h, table + (size_t)id000 * PHONO_TABLE_COLS, h->abc);
   return PHONO_OK;
 }
 
@@ -670,6 +680,28 @@ int phono_read_surface(phono_handle* h, int first, int count, void* host_out) {
   return PHONO_OK;
 }
 
+int phono_set_steps_done(phono_handle* h, int steps) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (steps < 0 || steps > h->nsrc) return fail(PHONO_ERR_ARG, "steps must be in 0..(source samples set)");
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(h->step_base, &steps, sizeof(int), cudaMemcpyHostToDevice));
+  h->steps_done = steps;
+  return PHONO_OK;
+}
+
+int phono_upload_surface(phono_handle* h, int first, int count, const void* host_in) {
+  if (!h || (!host_in && count > 0)) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (first < 0 || count < 0 || first + count > h->nrec_cap) return fail(PHONO_ERR_ARG, "record range out of bounds");
+  if (count == 0) return PHONO_OK;
+  size_t rec = (size_t)h->d.nx * h->d.ny * h->es;
+  CK(cudaMemcpyAsync((char*)h->surf + (size_t)first * rec, host_in, (size_t)count * rec, cudaMemcpyHostToDevice,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return PHONO_OK;
+}
+
 static int field_check(phono_handle* h, int field, const void* host, size_t bytes, void** dev) {
   if (!h || !host) return fail(PHONO_ERR_ARG, "NULL argument");
   if (field < 0 || field > PHONO_FIELD_CZ) return fail(PHONO_ERR_ARG, "unknown field");
@@ -752,6 +784,48 @@ int phono_set_materials(phono_handle* h, const uint8_t* mat, const double* table
   if (rc) return rc;
   // the absorbing-face coefficients are kernel arguments baked into the graph
   if (h->graph) {
+    CK(cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return PHONO_OK;
+}
+
+int phono_set_lattice(phono_handle* h, const phono_lattice* lat, const double* table, int nmat) {
+  if (!h || !lat || !table || !lat->radius || !lat->kind) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (nmat < 1 || nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
+  if (lat->pitch < 1 || lat->ncx < 1 || lat->ncy < 1) return fail(PHONO_ERR_ARG, "pitch and cell counts must be >= 1");
+  if (lat->host < 0 || lat->host >= nmat) return fail(PHONO_ERR_ARG, "host material id out of range");
+  const int ncell = lat->ncx * lat->ncy;
+  for (int q = 0; q < ncell; q++) {
+    if (lat->kind[q] >= nmat) return fail(PHONO_ERR_ARG, "hole material id out of range");
+    if (!(lat->radius[q] >= 0.0) || !std::isfinite(lat->radius[q])) return fail(PHONO_ERR_ARG, "radius must be finite and >= 0");
+  }
+  for (int q = 0; q < nmat * PHONO_TABLE_COLS; q++)
+    if (!std::isfinite(table[q])) return fail(PHONO_ERR_ARG, "material table holds a non-finite value");
+  for (int q = 0; q < nmat; q++)
+    if (!(table[q * PHONO_TABLE_COLS + 12] > 0.0)) return fail(PHONO_ERR_ARG, "density must be > 0");
+  CK(cudaStreamSynchronize(h->stream));
+  double* d_r = nullptr;
+  uint8_t* d_k = nullptr;
+  CK(cudaMalloc(&d_r, sizeof(double) * ncell));
+  cudaError_t e = cudaMalloc(&d_k, ncell);
+  if (e == cudaSuccess) e = cudaMemcpy(d_r, lat->radius, sizeof(double) * ncell, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_k, lat->kind, ncell, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_lattice_ids(h->mat, h->g, lat->pitch, lat->ncx, lat->ncy, d_r, d_k, lat->depth,
+                                               (uint8_t)lat->host, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d_r);
+  cudaFree(d_k);
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("lattice ids: ") + cudaGetErrorString(e));
+  // node (0, 0, 0): inside the hole of cell (0, 0) only if its radius exceeds
+  // the distance to the cell centre (the same test as the kernel's)
+  const double c0 = 0.5 * lat->pitch, r0 = lat->radius[0];
+  const int id000 = (c0 * c0 + c0 * c0 < r0 * r0 && lat->depth >= 0) ? lat->kind[0] : lat->host;
+  int rc = upload_table(h, table, nmat, id000);
+  if (rc) return rc;
+  if (h->graph) {  // the absorbing-face coefficients are kernel arguments baked into the graph
     CK(cudaStreamSynchronize(h->stream));
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;

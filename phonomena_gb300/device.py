@@ -69,11 +69,14 @@ class DeviceSimulation:
         self._h = h
         self.tile_j = int(tile_j) or 8
         self.x_segment = int(x_segment) or 32
+        self.surface_mode, self.bc, self.source_mode = surface_mode, bc, source_mode
+        self._source = None
 
     # -- control ----------------------------------------------------------
     def set_source(self, samples):
         s = np.ascontiguousarray(samples, dtype=np.float64)
         check(self._L.phono_set_source(self._h, s.ctypes.data, s.size))
+        self._source = s
 
     def step(self, n):
         check(self._L.phono_step(self._h, int(n)))
@@ -95,6 +98,29 @@ class DeviceSimulation:
         check(self._L.phono_set_tiling(self._h, int(tile_j), int(x_segment)))
         self.tile_j = int(tile_j) or self.tile_j
         self.x_segment = int(x_segment) or self.x_segment
+
+    def set_lattice(self, lat, table):
+        """Material ids built on the device from a hole lattice (crystal.lattice)
+        and a new table; same ids as set_materials(crystal.ids_from_lattice(...))."""
+        radius = np.ascontiguousarray(lat["radius"], dtype=np.float64)
+        kind = np.ascontiguousarray(lat["kind"], dtype=np.uint8)
+        if radius.ndim != 2 or kind.shape != radius.shape:
+            raise ValueError("radius and kind must be (ncx, ncy) arrays of one shape")
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 13)
+        d = _lib.PhonoLattice(int(lat["pitch"]), radius.shape[0], radius.shape[1], radius.ctypes.data,
+                              kind.ctypes.data, int(lat["depth"]), int(lat.get("host", 0)))
+        check(self._L.phono_set_lattice(self._h, ctypes.byref(d), t.ctypes.data, t.shape[0]))
+        self.mat = None  # ids live on the device; host_ids() rebuilds them when asked
+        self._lattice = lat
+        self.table = t
+
+    def host_ids(self):
+        """The node material ids on the host (rebuilt from the lattice if they were made on the device)."""
+        if self.mat is None:
+            from .crystal import ids_from_lattice
+
+            self.mat = ids_from_lattice((self.nx, self.ny, self.nz), self._lattice)
+        return self.mat
 
     @property
     def stream_ptr(self):
@@ -145,6 +171,60 @@ class DeviceSimulation:
         if a.shape != field_shape(self.nx, self.ny, self.nz, f % 3):
             raise ValueError(f"{field} must have shape {field_shape(self.nx, self.ny, self.nz, f % 3)}")
         check(self._L.phono_upload(self._h, f, a.ctypes.data, a.nbytes))
+
+    # -- checkpoint / resume ------------------------------------------------
+    @property
+    def state_fields(self):
+        """Fields that make up the state of this scheme (all others are derived)."""
+        if self.precision == "f64":
+            return ("ux", "uy", "uz", "ux_old", "uy_old", "uz_old")
+        return ("ux", "uy", "uz", "vx", "vy", "vz", "cx", "cy", "cz")
+
+    def checkpoint(self):
+        """Everything needed to resume this run on another handle: the state
+        fields, the step count, the surface records so far and the inputs."""
+        self.sync()
+        ck = {k: self.download(k) for k in self.state_fields}
+        ck["steps_done"] = np.array(self.steps_done)
+        ck["surface"] = self.read_surface()
+        ck["ids"] = self.host_ids()
+        ck["table"] = self.table
+        ck["source"] = self._source if self._source is not None else np.zeros(0)
+        for k, v in self._sp.items():
+            ck[k] = v
+        ck["meta"] = np.array([self.dt, self.max_steps, self.record_every, self.tile_j, self.x_segment], np.float64)
+        ck["modes"] = np.array([self.precision, self.surface_mode, self.bc, self.source_mode])
+        return ck
+
+    def save_checkpoint(self, path):
+        np.savez(path, **self.checkpoint())
+
+    def restore(self, ck):
+        """Resume from a checkpoint of a run with the same description and source."""
+        steps = int(ck["steps_done"])
+        check(self._L.phono_set_steps_done(self._h, steps))  # selects the buffers the fields go to
+        for k in self.state_fields:
+            self.upload(k, ck[k])
+        surf = np.ascontiguousarray(ck["surface"], dtype=self.dtype)
+        if surf.shape[0]:
+            check(self._L.phono_upload_surface(self._h, 0, surf.shape[0], surf.ctypes.data))
+
+    @classmethod
+    def from_checkpoint(cls, ck):
+        """A new simulation resumed from a checkpoint (dict or .npz path)."""
+        if not isinstance(ck, dict):
+            with np.load(ck) as f:
+                ck = {k: f[k] for k in f.files}
+        dt, max_steps, record_every, tile_j, x_segment = ck["meta"]
+        precision, surface_mode, bc, source_mode = (str(x) for x in ck["modes"])
+        sp = {k: ck[k] for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")}
+        sim = cls(sp, ck["ids"], ck["table"], float(dt), precision=precision, surface_mode=surface_mode, bc=bc,
+                  source_mode=source_mode, max_steps=int(max_steps), record_every=int(record_every),
+                  tile_j=int(tile_j), x_segment=int(x_segment))
+        if ck["source"].size:
+            sim.set_source(ck["source"])
+        sim.restore(ck)
+        return sim
 
     def energy(self):
         out = np.zeros(2, np.float64)

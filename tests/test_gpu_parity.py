@@ -237,3 +237,67 @@ def test_plugin_solver_test_defaults(gpu_lib):
         assert G.matches(d, key, getattr(s.g, key))
     assert G.matches(d, "surf", s.surface)
     s.release()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_checkpoint_resume_bit_exact(gpu_lib, tmp_path, precision):
+    """A run stopped at step 130, saved to a file and resumed in a new handle
+    ends bit-identical to the run that never stopped (fields and records)."""
+    from phonomena_gb300 import crystal
+    from phonomena_gb300.device import DeviceSimulation
+
+    spec = crystal.CrystalSpec(cells=(40, 36, 24), lattice=8, radius=(0.2, 0.4), tungsten_frac=0.3, seed=5,
+                               steps=300)
+    g, m = crystal.build(spec)
+    src = crystal.sin_source(spec.freq, m.dt, 300)
+
+    def make():
+        s = DeviceSimulation(g.spacing(), m.ids, m.table, m.dt, precision=precision, surface_mode="corrected",
+                             max_steps=300, record_every=10, tile_j=8, x_segment=16)
+        s.set_source(src)
+        return s
+
+    with make() as ref:
+        ref.step(300)
+        ref.sync()
+        want = {k: ref.download(k) for k in ref.state_fields}
+        want_surf = ref.read_surface()
+    with make() as a:
+        a.step(130)
+        a.save_checkpoint(tmp_path / "ck.npz")
+    with DeviceSimulation.from_checkpoint(tmp_path / "ck.npz") as b:
+        assert b.steps_done == 130
+        b.step(170)
+        b.sync()
+        for k, v in want.items():
+            assert np.array_equal(b.download(k), v), k
+        assert np.array_equal(b.read_surface(), want_surf)
+
+
+@pytest.mark.parametrize("cells,a,seed", [((40, 36, 24), 8, 1), ((64, 50, 20), 12, 2), ((33, 47, 30), 16, 3)])
+def test_device_lattice_ids_equal_host_ids(gpu_lib, cells, a, seed):
+    """Material ids built by the lattice kernel give the same run, bit for bit,
+    as the host-built ids (FP32K: any id difference shows in the fields)."""
+    from phonomena_gb300 import crystal
+    from phonomena_gb300.device import DeviceSimulation
+
+    spec = crystal.CrystalSpec(cells=cells, lattice=a, radius=(0.2, 0.45), tungsten_frac=0.4, seed=seed, depth=7,
+                               steps=40)
+    g, m = crystal.build(spec)
+    lat = crystal.lattice(spec)
+    src = crystal.sin_source(spec.freq, m.dt, 40)
+    out = []
+    for mode in ("host", "device"):
+        with DeviceSimulation(g.spacing(), np.zeros_like(m.ids), m.table, m.dt, precision="f32k",
+                              surface_mode="corrected", max_steps=40, record_every=5) as sim:
+            if mode == "host":
+                sim.set_materials(crystal.ids_from_lattice(spec.nodes, lat), m.table)
+            else:
+                sim.set_lattice(lat, m.table)
+            sim.set_source(src)
+            sim.step(40)
+            sim.sync()
+            out.append([sim.download(k) for k in ("ux", "uy", "uz")] + [sim.read_surface()])
+    assert np.array_equal(crystal.ids_from_lattice(spec.nodes, lat), m.ids)
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
