@@ -35,7 +35,6 @@ import numpy as np
 CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 TILE_J = (4, 8, 16)
 X_SEGMENTS = (12, 16, 20, 24, 28, 32, 40, 48, 64)
-DEFAULT = (8, 32)
 _HOST_ROW = np.array([[224e9, 64e9, 64e9, 64e9, 224e9, 64e9, 64e9, 64e9, 224e9, 80e9, 80e9, 80e9, 2330.0]])
 
 

@@ -496,7 +496,9 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   h->mat_bytes = (size_t)(nx + 2) * h->g.msx;
 
   // tiles
-  if (set_tiling(h, d->tile_j ? d->tile_j : 8, d->x_segment ? d->x_segment : 32)) {
+  // default tile: height 4 for FP32 (one row a thread), 8 for FP64; 24 planes
+  // per segment (the tuned shapes of the 256x256x128 crystal on GB300)
+  if (set_tiling(h, d->tile_j ? d->tile_j : (d->precision == PHONO_F32K ? 4 : 8), d->x_segment ? d->x_segment : 24)) {
     std::string m_ = g_err;
     delete h;
     g_err = m_;

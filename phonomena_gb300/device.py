@@ -67,8 +67,8 @@ class DeviceSimulation:
         h = ctypes.c_void_p()
         check(L.phono_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
-        self.tile_j = int(tile_j) or 8
-        self.x_segment = int(x_segment) or 32
+        self.tile_j = int(tile_j) or (4 if precision == "f32k" else 8)
+        self.x_segment = int(x_segment) or 24
         self.surface_mode, self.bc, self.source_mode = surface_mode, bc, source_mode
         self._source = None
 

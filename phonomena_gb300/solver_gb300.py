@@ -21,7 +21,7 @@ Extra ``cfg`` keys (merged like solver_default.py:19):
   bc            'absorbing' (reference faces) | 'rigid'
   source_mode   'line' (uz[0,:,0], reference) | 'wall' (uz[0,:,:])
   record_every  surface uz[:,:,0] sampling period in steps (0 = off)
-  tile_j, x_segment  kernel tile shape (0 = autotuned)
+  tile_j, x_segment  kernel tile shape (0: tuned once per mesh above 2M nodes, else the default)
 """
 from __future__ import annotations
 
@@ -43,6 +43,7 @@ except Exception:  # standalone
 from .device import DeviceSimulation
 from .model import solver_inputs
 
+TUNE_MIN_NODES = 2_000_000  # below this the default tile shape is used without tuning
 logger = logging.getLogger(__name__)
 
 cfg = {"precision": "f64", "surface_mode": "reference", "bc": "absorbing", "source_mode": "line",
@@ -77,10 +78,15 @@ class Solver(_Base):
         spacing, ids, table, dt = solver_inputs(self.g, self.m)
         c = self.cfg
         self.record_every = int(c.get("record_every", 0) or 0)
+        tj, xs = int(c.get("tile_j", 0) or 0), int(c.get("x_segment", 0) or 0)
+        if not tj and ids.size >= TUNE_MIN_NODES:  # large meshes: the tuner's shape (cached per mesh)
+            from . import autotune
+
+            tj, xs = autotune.tune(spacing, ids, table, dt, precision=c["precision"])
         self.sim = DeviceSimulation(spacing, ids, table, dt, precision=c["precision"],
                                     surface_mode=c["surface_mode"], bc=c["bc"], source_mode=c["source_mode"],
                                     max_steps=max(int(self.t), 1), record_every=self.record_every,
-                                    tile_j=int(c.get("tile_j", 0) or 0), x_segment=int(c.get("x_segment", 0) or 0))
+                                    tile_j=tj, x_segment=xs)
         wave_fn = {"sin": self.update_sin, "ricker": self.update_ricker}[c["wave"]]
         samples = np.array([wave_fn(tt=tt, **c["wave_args"]) for tt in range(int(self.t))], dtype=np.float64)
         self.sim.set_source(samples)
