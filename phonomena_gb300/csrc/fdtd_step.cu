@@ -1,33 +1,38 @@
-// Fused elastic FDTD step for GB300 (sm_103a).
+// Elastic FDTD step for GB300 (sm_103a).
 //
-// One launch advances one time step of phonomena's staggered-grid solver
-// (simulation/base_solver.py:245-266).  The launch has two kinds of blocks:
+// One time step of phonomena's staggered-grid solver
+// (simulation/base_solver.py:245-266) is a tile launch and a face launch:
 //
-//  * tile blocks: a (TJ x 32) tile of the (y, z) plane marches along x over a
-//    segment of planes.  Planes of u (all three components, 1-node halo) and
-//    of the material ids stream into a 4-slot shared-memory ring through TMA
-//    (cp.async.bulk.tensor, completion on an mbarrier per slot), two planes
-//    ahead of the plane being computed.  Each iteration evaluates the six
-//    stresses of the current plane once (plus the halo stresses the
-//    neighbours need) into shared memory and writes the new displacement of
-//    the plane.  Stresses are never written to global memory; the pointwise
-//    state (u_old, or v and the Kahan term) is prefetched one plane ahead
-//    into registers.
+//  * tile blocks (tile_path.cuh, tile_rows.cuh): a (TJ x 32) tile of the
+//    (y, z) plane marches along x over a segment of planes.  Planes of u (all
+//    three components, 1-node halo), of the material ids and of the pointwise
+//    state of the own points (u_old, or v and the Kahan term) stream into a
+//    4-slot shared-memory ring through TMA (cp.async.bulk.tensor, completion
+//    on an mbarrier per slot).  Each iteration evaluates the six stresses of
+//    the current plane once (plus the halo stresses the neighbours need) into
+//    shared memory and writes the new state of the plane.  Stresses are never
+//    written to global memory.  The tile pass also writes the z = N face
+//    point above every (i, j) that is on no x / y face.
 //
-//  * face blocks: one thread per point of the four absorbing faces
-//    (x=N, y=0, y=N, z=N; simulation/base_solver.py:540-554).  The reference
+//  * face points (fdtd_face_kernel, a second launch; for ny == 3, extra
+//    blocks of the same launch): the x = N, y = 0, y = N faces and the z = N
+//    points on them (simulation/base_solver.py:540-554).  The reference
 //    applies the faces one after another, each reading the plane next to it
 //    as left by the earlier faces; the final value of a face point is thus a
 //    chain of at most four face formulas ending at the interior value of one
-//    point q.  The face thread walks that chain and evaluates q's interior
-//    value itself from the input state, so faces need no second pass.
+//    point q.  The face thread walks that chain from q's new value (written
+//    by the tile pass; evaluated from the input state in the one-launch form).
 //
-// Two arithmetic schemes share this structure:
+// Three arithmetic schemes share this structure:
 //  F64  - the reference leapfrog u' = (2u - u_old) + (dt^2/P) * div T with the
 //         reference's IEEE operation order (explicit _rn intrinsics, true
 //         division), bit-identical to the reference CPU solver.
 //  F32K - FP32 velocity form v' = v + (dt/P) div T, u' = u + dt v' with a
 //         Kahan-compensated displacement sum; explicit fmaf only.
+//  F64V - the F32K scheme in FP64.
+//
+// Batches (batch_step_kernel and friends) run the same tile pass over the
+// (instance, tile) work items of many instances in one persistent launch.
 #include <cstdio>
 #include "fdtd_common.cuh"
 
@@ -407,26 +412,16 @@ struct GlobalFetch {
   }
 };
 
+// Geometry of one ring slot of a (TJ x 32) tile: a u component tile is
+// TJ+2 rows (1-row halo) of KW values starting KB before the tile's first z
+// point; the three components follow each other (CW apart); SU and SM are the
+// slot strides of u and of the material ids, rounded to 128 bytes.
 template <class R, int TJ>
-struct TileFetch {
+struct TileShape {
   static constexpr int KW = Lay<R>::KW, KB = Lay<R>::KB;
   static constexpr int CW = (TJ + 2) * KW;                       // component stride in a slot
   static constexpr int SU = ((3 * CW * (int)sizeof(R) + 127) / 128) * 128 / (int)sizeof(R);  // slot stride
   static constexpr int SM = (((TJ + 2) * MKW + 127) / 128) * 128;                               // mat slot stride
-  const R* uring;
-  const uint8_t* mring;
-  const R* tab;
-  int j0, k0, ibase;
-  __device__ __forceinline__ int slot(int i) const { return (i - ibase) & (NSLOT - 1); }
-  __device__ __forceinline__ int loc(int i, int j, int k) const {
-    return slot(i) * SU + (j - j0 + 1) * KW + (k - k0 + KB);
-  }
-  __device__ __forceinline__ R x(int i, int j, int k) const { return uring[loc(i, j, k)]; }
-  __device__ __forceinline__ R y(int i, int j, int k) const { return uring[loc(i, j, k) + CW]; }
-  __device__ __forceinline__ R z(int i, int j, int k) const { return uring[loc(i, j, k) + 2 * CW]; }
-  __device__ __forceinline__ const R* row(int i, int j, int k) const {
-    return tab + 16 * mring[slot(i) * SM + (j - j0 + 1) * MKW + (k - k0 + MKOFF)];
-  }
 };
 
 // interior (V0) value of u_new at a point, evaluated from global memory
@@ -582,7 +577,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
 template <class S, int TJ>
 struct SmemPlan {
   using R = typename S::R;
-  using TF = TileFetch<R, TJ>;
+  using TF = TileShape<R, TJ>;
   static constexpr int W = TK + 2, PL = W * (TJ + 2);
   static constexpr int NPW = S::kahan ? 2 : 1;  // pointwise arrays: v and c, or u_old
   static constexpr int PWC = TJ * TK;           // one component of a pointwise tile

@@ -20,7 +20,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
                                            const int tid, const int b, const StepArgs<typename S::R>* maps) {
   using R = typename S::R;
   using P = SmemPlan<S, TJ>;
-  using TF = TileFetch<R, TJ>;
+  using TF = TileShape<R, TJ>;
   constexpr int NT = TK * TJ;
   constexpr int W = P::W, PL = P::PL;
   constexpr int KW = TF::KW, KB = TF::KB, CW = TF::CW, SU = TF::SU, SM = TF::SM;

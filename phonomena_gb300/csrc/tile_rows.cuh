@@ -23,7 +23,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
                                            const int tid, const int b, const StepArgs<typename S::R>* maps) {
   using R = typename S::R;
   using P = SmemPlan<S, TJ>;
-  using TF = TileFetch<R, TJ>;
+  using TF = TileShape<R, TJ>;
   constexpr int JR = RowsPerThread<S, TJ>::value;
   constexpr int NT = TK * TJ / JR;
   constexpr int W = P::W, PL = P::PL;
