@@ -89,7 +89,7 @@ typedef struct phono_desc {
   int max_steps;                 /* capacity: source samples and surface records */
   int record_every;              /* record uz[:, :, 0] after every k-th step; 0 = off */
   int tile_j;                    /* tile height along y: 4, 8 or 16; 0 = default (F32K 4, else 8) */
-  int x_segment;                 /* planes per tile column segment; 0 = default (24) */
+  int x_segment;                 /* planes per block segment; -L: L-plane segments, the last 2L planes in four shorter ones; 0 = default (24) */
 } phono_desc;
 
 typedef struct phono_handle phono_handle;

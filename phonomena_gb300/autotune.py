@@ -35,6 +35,7 @@ import numpy as np
 CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 TILE_J = (4, 8, 16)
 X_SEGMENTS = (12, 16, 20, 24, 28, 32, 40, 48, 64)
+X_TAPERED = (16, 20, 24, 28, 32, 48)  # -L: L-plane segments shortening towards the end (see phono_desc.x_segment)
 _HOST_ROW = np.array([[224e9, 64e9, 64e9, 64e9, 224e9, 64e9, 64e9, 64e9, 224e9, 80e9, 80e9, 80e9, 2330.0]])
 
 
@@ -90,7 +91,8 @@ def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None,
             return tuple(hit["best"])
     if steps is None:
         steps = 48 if precision == "f32k" else 12
-    cands = candidates or [(tj, xs) for tj in TILE_J for xs in X_SEGMENTS]
+    cands = candidates or ([(tj, xs) for tj in TILE_J for xs in X_SEGMENTS] +
+                           [(tj, -xs) for tj in TILE_J for xs in X_TAPERED])
     results = []
     sim = _scratch(shape, precision, (steps + 12) * len(cands) + 12)
     try:

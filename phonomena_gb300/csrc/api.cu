@@ -79,6 +79,7 @@ struct phono_handle {
   double abc[8] = {};
   int tj = 8, xseg = 64, ntj = 0, ntk = 0, nseg = 0, n_tile = 0, n_face = 0, separate_faces = 1;
   FaceTable faces{};
+  std::vector<int> seg_start;  // first plane of each x segment, + nx-1
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -242,6 +243,7 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.ntj = h->ntj;
   a.ntk = h->ntk;
   a.nseg = h->nseg;
+  for (int q = 0; q <= SEG_TABLE && q < (int)h->seg_start.size(); q++) a.seg_start[q] = h->seg_start[q];
   a.xseg = h->xseg;
   a.n_tile_blocks = h->n_tile;
   a.faces = h->faces;
@@ -303,7 +305,7 @@ static int check_desc(const phono_desc* d) {
   if (d->max_steps < 0 || d->record_every < 0) return fail(PHONO_ERR_ARG, "max_steps and record_every must be >= 0");
   if (!(d->dt > 0.0) || !std::isfinite(d->dt)) return fail(PHONO_ERR_ARG, "dt must be finite and > 0");
   if (d->tile_j != 0 && d->tile_j != 4 && d->tile_j != 8 && d->tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
-  if (d->x_segment < 0) return fail(PHONO_ERR_ARG, "x_segment must be >= 0");
+  if (d->x_segment < -4096) return fail(PHONO_ERR_ARG, "x_segment out of range");
   for (int q = 0; q < d->nmat * PHONO_TABLE_COLS; q++)
     if (!std::isfinite(d->table[q])) return fail(PHONO_ERR_ARG, "material table holds a non-finite value");
   for (int q = 0; q < d->nmat; q++)
@@ -364,9 +366,30 @@ static void* field_ptr(phono_handle* h, int field) {
 
 // Tile decomposition of a handle: tile_j rows x 32 z-points per block, the
 // x axis cut into segments of x_segment planes, and the face-pass work list.
+// x_segment > 0: segments of x_segment planes (the last one shorter).
+// x_segment = -L: tapered segments -- L planes while more than 2L planes are
+// left, then the rest in four nearly equal parts -- so that the blocks a
+// launch dispatches last are short and the tail of the last wave is short.
+static std::vector<int> segment_starts(int planes, int xseg) {
+  std::vector<int> st{0};
+  if (xseg > 0) {
+    for (int p = xseg; p < planes; p += xseg) st.push_back(p);
+  } else {
+    const int len = -xseg;
+    int p = 0;
+    while (planes - p > 2 * len) st.push_back(p += len);
+    const int rem = planes - p, parts = rem >= 4 ? 4 : (rem > 0 ? rem : 0);
+    for (int q = 1; q < parts; q++) st.push_back(p + (int)((long long)rem * q / parts));
+  }
+  st.push_back(planes);
+  return st;
+}
+
 static int set_tiling(phono_handle* h, int tj, int xseg) {
   const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
-  const int ntj = (ny - 1 + tj - 1) / tj, ntk = (nz - 1 + TK - 1) / TK, nseg = (nx - 1 + xseg - 1) / xseg;
+  std::vector<int> starts = segment_starts(nx - 1, xseg);
+  const int ntj = (ny - 1 + tj - 1) / tj, ntk = (nz - 1 + TK - 1) / TK, nseg = (int)starts.size() - 1;
+  if (xseg < 0 && nseg > SEG_TABLE) return fail(PHONO_ERR_ARG, "tapered x segments: more than 64 segments");
   long long ntile = (long long)ntj * ntk * nseg;
   // face points left to the face pass, per component: z=N only where it meets
   // an x / y face (2*ex + ey-2; the tile pass writes the rest), y=N and y=0
@@ -386,6 +409,7 @@ static int set_tiling(phono_handle* h, int tj, int xseg) {
   if (ntile + nface > 0x7fffffffLL || acc > 0x7fffffffLL) return fail(PHONO_ERR_ARG, "grid too large for one launch");
   h->tj = tj;
   h->xseg = xseg;
+  h->seg_start = starts;
   h->ntj = ntj;
   h->ntk = ntk;
   h->nseg = nseg;
@@ -843,7 +867,7 @@ int phono_set_tiling(phono_handle* h, int tile_j, int x_segment) {
   if (tile_j == 0) tile_j = h->tj;
   if (x_segment == 0) x_segment = h->xseg;
   if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
-  if (x_segment < 0) return fail(PHONO_ERR_ARG, "x_segment must be >= 0");
+  if (x_segment < -4096) return fail(PHONO_ERR_ARG, "x_segment out of range");
   if (tile_j == h->tj && x_segment == h->xseg) return PHONO_OK;
   CK(cudaStreamSynchronize(h->stream));
   const int p = h->d.precision;

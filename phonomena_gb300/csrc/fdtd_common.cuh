@@ -28,6 +28,7 @@ namespace phono {
 
 constexpr int TK = 32;      // tile width along z (the contiguous axis): one warp
 constexpr int NSLOT = 4;    // planes in the shared-memory ring
+constexpr int SEG_TABLE = 64;  // x segments a launch describes by table (more: uniform segments)
 constexpr int MKOFF = 8;    // material front pad in k (bytes)
 constexpr int MKW = 48;     // material tile width in k (bytes): k0-8 .. k0+40
 constexpr int TAB_ROWS_MAX = 256;  // material rows a table may hold (uint8 ids)
@@ -100,6 +101,9 @@ struct StepArgs {
   int surface_mode, bc, source_mode;
   // tile decomposition of the box [0,nx-1) x [0,ny-1) x [0,nz-1)
   int ntj, ntk, nseg, xseg;
+  // first plane of each x segment (nseg + 1 entries) when nseg <= SEG_TABLE;
+  // the segment order is the launch order, so short segments can come last
+  int seg_start[SEG_TABLE + 1];
   int n_tile_blocks;
   FaceTable faces;
   int* __restrict__ err;  // device error flags: 1 non-finite surface value, 2 pipeline wait timed out

@@ -44,8 +44,8 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
   const int jt = rest % a.ntj;
   const int seg = rest / a.ntj;
   const int j0 = jt * TJ, k0 = kt * TK;
-  const int ib = seg * a.xseg;
-  const int ie = min(ib + a.xseg, nx - 1);
+  const int ib = a.nseg <= SEG_TABLE ? a.seg_start[seg] : seg * a.xseg;
+  const int ie = a.nseg <= SEG_TABLE ? a.seg_start[seg + 1] : min(ib + a.xseg, nx - 1);
   const int ibase = ib - 1;
   const int plast = ie + 1;  // last plane the segment reads
   const int tx = threadIdx.x, ty = threadIdx.y;

@@ -40,7 +40,7 @@ def test_f64_bit_exact_vs_reference(gpu_lib, name):
         assert G.matches(d, "surf", sim.read_surface()), f"{name}: surface differs from the reference"
 
 
-@pytest.mark.parametrize("tile_j,x_segment", [(4, 5), (8, 64), (16, 3), (8, 1)])
+@pytest.mark.parametrize("tile_j,x_segment", [(4, 5), (8, 64), (16, 3), (8, 1), (4, -8), (8, -3)])
 @pytest.mark.parametrize("name", ["small3_ref", "config1_void_corrected", "nonuniform_json"])
 def test_f64_tile_shapes_bit_exact(gpu_lib, name, tile_j, x_segment):
     d = G.load(name)
