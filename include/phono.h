@@ -255,6 +255,15 @@ void phono_batch_destroy(phono_batch *b);
  * time candidates on one handle.  No reference counterpart. */
 int phono_set_tiling(phono_handle *h, int tile_j, int x_segment);
 
+/* Tile height (0 keeps it) and an explicit list of x segments: n lengths in
+ * planes, dispatched in list order, each >= 1, adding up to nx - 1, n <= 64.
+ * A block marches one segment of one (y, z) tile, so the list sets how the
+ * launch's work is cut into blocks; long segments first and a shortening
+ * tail keep the last wave of blocks short.  phono_set_tiling(h, tj, 0) keeps
+ * the list.  Results do not depend on it.  No reference counterpart. */
+#define PHONO_MAX_SEGMENTS 64
+int phono_set_segments(phono_handle *h, int tile_j, const int *lengths, int n);
+
 /* Device time of the last phono_step call in milliseconds (CUDA events). */
 int phono_last_step_ms(phono_handle *h, float *ms);
 

@@ -27,7 +27,7 @@ EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
            "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
            "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
-           "phono_batch_destroy", "phono_set_tiling", "phono_footprint", "phono_set_steps_done",
+           "phono_batch_destroy", "phono_set_tiling", "phono_set_segments", "phono_footprint", "phono_set_steps_done",
            "phono_upload_surface", "phono_set_lattice",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
@@ -111,6 +111,7 @@ def load(path: Path | None = None):
         "phono_batch_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_batch_destroy": (None, [vp]),
         "phono_set_tiling": (ci, [vp, ci, ci]),
+        "phono_set_segments": (ci, [vp, ci, vp, ci]),
         "phono_set_steps_done": (ci, [vp, ci]),
         "phono_upload_surface": (ci, [vp, ci, ci, vp]),
         "phono_set_lattice": (ci, [vp, ctypes.POINTER(PhonoLattice), vp, ci]),

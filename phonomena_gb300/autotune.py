@@ -21,7 +21,9 @@ tile_j sets the block (a 32 x tile_j tile: 32 x tile_j threads at height 4,
 two rows a thread at 8 and 16 in FP32; shared memory per block); the x
 segment sets how many x planes a block marches and thereby the number of
 blocks (several waves of the 152 SMs vs. the re-read of two halo planes per
-segment).
+segment).  Blocks are dispatched segment by segment, so segments that
+shorten towards the end of the list (tapered or listed) make the blocks that
+run while the GPU drains at the end of a launch short.
 """
 from __future__ import annotations
 
@@ -36,6 +38,10 @@ CACHE = Path(__file__).resolve().parent / "_build" / "autotune.json"
 TILE_J = (4, 8, 16)
 X_SEGMENTS = (12, 16, 20, 24, 28, 32, 40, 48, 64)
 X_TAPERED = (16, 20, 24, 28, 32, 48)  # -L: L-plane segments shortening towards the end (see phono_desc.x_segment)
+# listed segments (phono_set_segments): L-plane segments, then one of these
+# shortening tails, so that the last blocks of a launch are short
+LISTED_L = (24, 28, 30, 32, 36)
+TAILS = ((16, 12, 8, 6, 4), (10, 8, 6, 4, 4), (12, 8, 4, 4, 4), (20, 16, 12, 8, 4), (6, 6, 6, 6, 4, 4))
 _HOST_ROW = np.array([[224e9, 64e9, 64e9, 64e9, 224e9, 64e9, 64e9, 64e9, 224e9, 80e9, 80e9, 80e9, 2330.0]])
 
 
@@ -81,6 +87,30 @@ def _scratch(shape, precision, max_steps, tile_j=8, x_segment=32):
     return sim
 
 
+def listed_segments(planes, length, tail):
+    """Segment lengths: length-plane segments, then the tail; the planes left
+    over are spread over the long segments.  None if they do not fit."""
+    rest = planes - sum(tail)
+    full = rest // length if rest > 0 else 0
+    if full < 1 or full + len(tail) > 64:
+        return None
+    extra = rest - full * length
+    return tuple(length + extra // full + (1 if q < extra % full else 0) for q in range(full)) + tuple(tail)
+
+
+def candidates_for(shape, tile_js=TILE_J):
+    """(tile_j, x_segment) candidates of a mesh: even, tapered and listed segments."""
+    planes = int(shape[0]) - 1
+    cands = [(tj, xs) for tj in tile_js for xs in X_SEGMENTS] + [(tj, -xs) for tj in tile_js for xs in X_TAPERED]
+    for tj in tile_js:
+        for length in LISTED_L:
+            for tail in TAILS:
+                seg = listed_segments(planes, length, tail)
+                if seg is not None and (tj, seg) not in cands:
+                    cands.append((tj, seg))
+    return cands
+
+
 def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None, use_cache=True, verbose=False):
     """Best (tile_j, x_segment) for this mesh and scheme; times each candidate."""
     shape = tuple(int(s) for s in np.shape(mat))
@@ -88,11 +118,11 @@ def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None,
     if use_cache:
         hit = _load().get(key)
         if hit:
-            return tuple(hit["best"])
+            tj, xs = hit["best"]
+            return int(tj), (tuple(xs) if isinstance(xs, list) else int(xs))
     if steps is None:
         steps = 48 if precision == "f32k" else 12
-    cands = candidates or ([(tj, xs) for tj in TILE_J for xs in X_SEGMENTS] +
-                           [(tj, -xs) for tj in TILE_J for xs in X_TAPERED])
+    cands = candidates or candidates_for(shape)
     results = []
     sim = _scratch(shape, precision, (steps + 12) * len(cands) + 12)
     try:
@@ -107,11 +137,12 @@ def tune(spacing, mat, table, dt, precision="f32k", steps=None, candidates=None,
                 print(f"autotune {precision} {shape} tile_j={tj} x_segment={xs}: {ms:.4f} ms/step")
     finally:
         sim.close()
-    results.sort()
+    results.sort(key=lambda r: r[0])
     best = (results[0][1], results[0][2])
     if use_cache:
-        _store(key, {"best": list(best), "ms_per_step": results[0][0],
-                     "all": [[tj, xs, round(ms, 5)] for ms, tj, xs in results]})
+        _store(key, {"best": [best[0], list(best[1]) if isinstance(best[1], tuple) else best[1]],
+                     "ms_per_step": results[0][0],
+                     "all": [[tj, list(xs) if isinstance(xs, tuple) else xs, round(ms, 5)] for ms, tj, xs in results]})
     return best
 
 

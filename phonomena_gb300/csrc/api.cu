@@ -1,5 +1,6 @@
 // C ABI of libphono_gpu.so (declared in include/phono.h).
 #include <cmath>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -385,11 +386,14 @@ static std::vector<int> segment_starts(int planes, int xseg) {
   return st;
 }
 
-static int set_tiling(phono_handle* h, int tj, int xseg) {
+// h->xseg of a handle whose segments were given as a list (phono_set_segments)
+constexpr int kExplicitSegments = INT_MIN;
+
+// tile height tj and x segments starting at starts[0..n) (+ nx-1 at the end)
+static int apply_tiling(phono_handle* h, int tj, int xseg, const std::vector<int>& starts) {
   const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
-  std::vector<int> starts = segment_starts(nx - 1, xseg);
   const int ntj = (ny - 1 + tj - 1) / tj, ntk = (nz - 1 + TK - 1) / TK, nseg = (int)starts.size() - 1;
-  if (xseg < 0 && nseg > SEG_TABLE) return fail(PHONO_ERR_ARG, "tapered x segments: more than 64 segments");
+  if (xseg <= 0 && nseg > SEG_TABLE) return fail(PHONO_ERR_ARG, "tapered or listed x segments: more than 64 segments");
   long long ntile = (long long)ntj * ntk * nseg;
   // face points left to the face pass, per component: z=N only where it meets
   // an x / y face (2*ex + ey-2; the tile pass writes the rest), y=N and y=0
@@ -420,6 +424,10 @@ static int set_tiling(phono_handle* h, int tj, int xseg) {
   // chain end of a face point can itself be a face point only when ny == 3
   h->separate_faces = ny >= 4 ? 1 : 0;
   return PHONO_OK;
+}
+
+static int set_tiling(phono_handle* h, int tj, int xseg) {
+  return apply_tiling(h, tj, xseg, segment_starts(h->d.nx - 1, xseg));
 }
 
 // TMA descriptors: a 4-D (k, j, i, array) map over the u allocation with a
@@ -861,24 +869,23 @@ int phono_set_lattice(phono_handle* h, const phono_lattice* lat, const double* t
 
 void* phono_stream(phono_handle* h) { return h ? (void*)h->stream : nullptr; }
 
-int phono_set_tiling(phono_handle* h, int tile_j, int x_segment) {
-  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
-  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
-  if (tile_j == 0) tile_j = h->tj;
-  if (x_segment == 0) x_segment = h->xseg;
-  if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
-  if (x_segment < -4096) return fail(PHONO_ERR_ARG, "x_segment out of range");
-  if (tile_j == h->tj && x_segment == h->xseg) return PHONO_OK;
+// switch a handle to tile height tj and the given x segments, keeping the old
+// shape if the new one cannot be set up
+static int retile(phono_handle* h, int tj, int xseg, const std::vector<int>& starts) {
+  if (tj == h->tj && starts == h->seg_start) {
+    h->xseg = xseg;
+    return PHONO_OK;
+  }
   CK(cudaStreamSynchronize(h->stream));
   const int p = h->d.precision;
-  CK(p == PHONO_F64 ? configure_step_f64(tile_j)
-                    : (p == PHONO_F64V ? configure_step_f64v(tile_j) : configure_step_f32k(tile_j)));
+  CK(p == PHONO_F64 ? configure_step_f64(tj) : (p == PHONO_F64V ? configure_step_f64v(tj) : configure_step_f32k(tj)));
   const int old_tj = h->tj, old_xs = h->xseg;
-  int rc = set_tiling(h, tile_j, x_segment);
+  const std::vector<int> old_starts = h->seg_start;
+  int rc = apply_tiling(h, tj, xseg, starts);
   if (!rc) rc = encode_tensor_maps(h);
   if (rc) {
     std::string m = g_err;
-    set_tiling(h, old_tj, old_xs);
+    apply_tiling(h, old_tj, old_xs, old_starts);
     encode_tensor_maps(h);
     g_err = m;
     return rc;
@@ -888,6 +895,35 @@ int phono_set_tiling(phono_handle* h, int tile_j, int x_segment) {
     h->graph = nullptr;
   }
   return PHONO_OK;
+}
+
+int phono_set_tiling(phono_handle* h, int tile_j, int x_segment) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (tile_j == 0) tile_j = h->tj;
+  if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
+  if (x_segment < -4096) return fail(PHONO_ERR_ARG, "x_segment out of range");
+  if (x_segment == 0)  // keep the current segments (a list included)
+    return retile(h, tile_j, h->xseg, h->seg_start);
+  return retile(h, tile_j, x_segment, segment_starts(h->d.nx - 1, x_segment));
+}
+
+int phono_set_segments(phono_handle* h, int tile_j, const int* lengths, int n) {
+  if (!h || !lengths) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (tile_j == 0) tile_j = h->tj;
+  if (tile_j != 4 && tile_j != 8 && tile_j != 16) return fail(PHONO_ERR_ARG, "tile_j must be 0, 4, 8 or 16");
+  if (n < 1 || n > PHONO_MAX_SEGMENTS) return fail(PHONO_ERR_ARG, "n must be 1..PHONO_MAX_SEGMENTS");
+  std::vector<int> starts{0};
+  long long sum = 0;
+  for (int q = 0; q < n; q++) {
+    if (lengths[q] < 1) return fail(PHONO_ERR_ARG, "segment lengths must be >= 1");
+    sum += lengths[q];
+    if (sum > h->d.nx - 1) break;
+    starts.push_back((int)sum);
+  }
+  if (sum != h->d.nx - 1) return fail(PHONO_ERR_ARG, "segment lengths must add up to nx - 1 planes");
+  return retile(h, tile_j, kExplicitSegments, starts);
 }
 
 void phono_destroy(phono_handle* h) { release(h); }
@@ -967,6 +1003,7 @@ static BatchArgs<float> batch_args(const phono_batch* b, int step_off) {
   return ba;
 }
 static_assert(sizeof(BatchArgs<float>) == sizeof(BatchArgs<double>), "batch argument layouts differ");
+static_assert(PHONO_MAX_SEGMENTS == SEG_TABLE, "segment list limit and the kernel table differ");
 
 // work items (costliest instances first), face-block prefix, active list
 static int batch_rebuild(phono_batch* b) {

@@ -58,6 +58,9 @@ class DeviceSimulation:
         self.record_every = int(record_every)
         self.max_steps = int(max_steps)
         self.dtype = np.float32 if precision == "f32k" else np.float64
+        segments = None
+        if np.ndim(x_segment):  # a list of segment lengths: set after creation
+            segments, x_segment = x_segment, 0
         d = _lib.PhonoDesc(
             self.nx, self.ny, self.nz,
             *(self._sp[k].ctypes.data for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")),
@@ -71,6 +74,12 @@ class DeviceSimulation:
         self.x_segment = int(x_segment) or 24
         self.surface_mode, self.bc, self.source_mode = surface_mode, bc, source_mode
         self._source = None
+        if segments is not None:
+            try:
+                self.set_tiling(0, segments)
+            except Exception:
+                self.close()
+                raise
 
     # -- control ----------------------------------------------------------
     def set_source(self, samples):
@@ -94,10 +103,19 @@ class DeviceSimulation:
         self.mat, self.table = m, t
 
     def set_tiling(self, tile_j=0, x_segment=0):
-        """Change the tile shape (0 keeps a value); results do not depend on it."""
-        check(self._L.phono_set_tiling(self._h, int(tile_j), int(x_segment)))
+        """Change the tile shape (0 keeps a value); results do not depend on it.
+
+        x_segment: planes per block segment, -L for tapered L-plane segments,
+        or a list of segment lengths adding up to nx - 1 (phono_set_segments).
+        """
+        if np.ndim(x_segment):
+            seg = np.ascontiguousarray(x_segment, dtype=np.int32)
+            check(self._L.phono_set_segments(self._h, int(tile_j), seg.ctypes.data, seg.size))
+            self.x_segment = tuple(int(v) for v in seg)
+        else:
+            check(self._L.phono_set_tiling(self._h, int(tile_j), int(x_segment)))
+            self.x_segment = int(x_segment) or self.x_segment
         self.tile_j = int(tile_j) or self.tile_j
-        self.x_segment = int(x_segment) or self.x_segment
 
     def set_lattice(self, lat, table):
         """Material ids built on the device from a hole lattice (crystal.lattice)
@@ -192,7 +210,10 @@ class DeviceSimulation:
         ck["source"] = self._source if self._source is not None else np.zeros(0)
         for k, v in self._sp.items():
             ck[k] = v
-        ck["meta"] = np.array([self.dt, self.max_steps, self.record_every, self.tile_j, self.x_segment], np.float64)
+        listed = isinstance(self.x_segment, tuple)
+        ck["meta"] = np.array([self.dt, self.max_steps, self.record_every, self.tile_j,
+                               0 if listed else self.x_segment], np.float64)
+        ck["segments"] = np.array(self.x_segment if listed else [], np.int32)
         ck["modes"] = np.array([self.precision, self.surface_mode, self.bc, self.source_mode])
         return ck
 
@@ -216,11 +237,14 @@ class DeviceSimulation:
             with np.load(ck) as f:
                 ck = {k: f[k] for k in f.files}
         dt, max_steps, record_every, tile_j, x_segment = ck["meta"]
+        segs = ck.get("segments")
+        if segs is not None and np.size(segs):
+            x_segment = tuple(int(v) for v in segs)
         precision, surface_mode, bc, source_mode = (str(x) for x in ck["modes"])
         sp = {k: ck[k] for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")}
         sim = cls(sp, ck["ids"], ck["table"], float(dt), precision=precision, surface_mode=surface_mode, bc=bc,
                   source_mode=source_mode, max_steps=int(max_steps), record_every=int(record_every),
-                  tile_j=int(tile_j), x_segment=int(x_segment))
+                  tile_j=int(tile_j), x_segment=x_segment if isinstance(x_segment, tuple) else int(x_segment))
         if ck["source"].size:
             sim.set_source(ck["source"])
         sim.restore(ck)

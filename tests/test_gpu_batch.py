@@ -125,6 +125,47 @@ def test_set_tiling_keeps_results(gpu_lib):
     s.close()
 
 
+def test_listed_segments_keep_results(gpu_lib):
+    """Explicit x segment lists (phono_set_segments) change nothing in the
+    results, alone and in a batch; bad lists are refused."""
+    from phonomena_gb300._lib import PhonoError
+    from phonomena_gb300.batch import Batch
+
+    cells = SHAPES[2]  # 65 x planes: segments add up to 64
+    ref = _sim(cells, 3, "f32k", 60)
+    ref.step(60)
+    want = _state(ref)
+    ref.close()
+
+    s = _sim(cells, 3, "f32k", 60, tile_j=4, x_segment=[20, 20, 10, 8, 4, 1, 1])
+    assert s.x_segment == (20, 20, 10, 8, 4, 1, 1)
+    s.step(23)
+    s.set_tiling(16, [1, 1, 1, 1, 60])
+    s.step(20)
+    s.set_tiling(8, 0)  # keeps the list
+    assert s.x_segment == (1, 1, 1, 1, 60)
+    s.step(17)
+    got = _state(s)
+    for a, e in zip(got[0], want[0]):
+        assert np.array_equal(a, e)
+    assert np.array_equal(got[1], want[1])
+    for bad in ([63], [65], [0, 64], [1] * 65, [-1, 65]):
+        with pytest.raises(PhonoError):
+            s.set_tiling(4, bad)
+    s.close()
+
+    s = _sim(cells, 3, "f32k", 60, tile_j=16, x_segment=[30, 20, 10, 4])
+    with Batch(1, precision="f32k", tile_j=16) as b:
+        b.add(s, 60)
+        b.step(60)
+        b.sync()
+    got = _state(s)
+    for a, e in zip(got[0], want[0]):
+        assert np.array_equal(a, e)
+    assert np.array_equal(got[1], want[1])
+    s.close()
+
+
 def test_handle_in_batch_is_guarded(gpu_lib):
     from phonomena_gb300._lib import PhonoError
     from phonomena_gb300.batch import Batch

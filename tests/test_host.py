@@ -167,3 +167,18 @@ def test_crystal_holes_clear_the_absorbing_faces():
         ids = crystal.material_ids(spec)
         assert not ids[-2:].any() and not ids[:, :2].any() and not ids[:, -2:].any(), spec.cells
         assert ids.any()  # the lattice is still there
+
+
+def test_listed_segment_candidates_cover_the_planes():
+    """The tuner's listed x segments add up to nx - 1 planes, fit the kernel's
+    64-entry table and end with their shortening tail."""
+    from phonomena_gb300 import autotune
+
+    for shape in ((257, 257, 129), (1025, 1025, 257), (65, 65, 33), (97, 161, 49), (9, 9, 9)):
+        for tj, xs in autotune.candidates_for(shape):
+            assert tj in autotune.TILE_J
+            if isinstance(xs, tuple):
+                assert sum(xs) == shape[0] - 1 and len(xs) <= 64 and min(xs) >= 1
+                assert any(xs[-len(t):] == t for t in autotune.TAILS)
+    assert autotune.listed_segments(256, 30, (16, 12, 8, 6, 4)) == (30,) * 7 + (16, 12, 8, 6, 4)
+    assert autotune.listed_segments(40, 36, (16, 12, 8, 6, 4)) is None
