@@ -36,7 +36,7 @@ def test_two_gloo_ranks_aggregate():
 
     port = _free_port()
     world = 2
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.start_processes(_worker, args=(world, port, out), nprocs=world, start_method="spawn", join=True)
         res = dict(out)
