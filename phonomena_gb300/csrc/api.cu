@@ -63,8 +63,9 @@ struct phono_handle {
   char* cbase = nullptr;   // F32K: 2 x 3 Kahan arrays
   CUtensorMap tm_u{}, tm_mat{}, tm_pw0{}, tm_pw1{};
   void* sp[6] = {};       // R spacings (F64 raw, F32K reciprocals)
-  double* sp64[6] = {};   // raw double spacings (energy)
+  double* rsp64[6] = {};  // reciprocal double spacings 1/fd, 1/sd (energy)
   double h_sp0[6] = {};   // first elements (raw)
+  DivTable dtab{};        // FP64 leapfrog: reciprocal pairs of the mesh's divisors (tab null: none)
   std::vector<double> sp_host[6];  // raw spacings (ABC coefficients)
   uint8_t* mat = nullptr;
   void* tab = nullptr;       // 16 R per material
@@ -199,6 +200,67 @@ static int upload_table(phono_handle* h, const double* table, int nmat, int id00
   return PHONO_OK;
 }
 
+// Divisor table of the FP64 leapfrog: one slot of {b, RN(1/b), RN((1-b*yh)/b), 0}
+// per distinct divisor b (every spacing value in [2^-40, 2^40], and 1.0), at
+// slot ((lo ^ hi) * mult) >> shift of b's 32-bit halves; mult and the slot
+// count are searched until no two divisors share a slot.  Empty slots hold a
+// bit pattern no divisor has, so they never match.  false: no table (too many
+// distinct values), every division stays the IEEE one.
+static bool build_div_table(const double* const arrs[6], const int lens[6], std::vector<double>& tbl, unsigned* mult,
+                            int* shift) {
+  std::vector<uint64_t> keys;
+  auto add = [&](double b) {
+    if (!(b >= std::ldexp(1.0, -40) && b <= std::ldexp(1.0, 40))) return;
+    uint64_t u;
+    std::memcpy(&u, &b, 8);
+    keys.push_back(u);
+  };
+  add(1.0);
+  for (int a = 0; a < 6; a++)
+    for (int q = 0; q < lens[a]; q++) add(arrs[a][q]);
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  auto slot_of = [](uint64_t u, unsigned m, int sh) {
+    return (((unsigned)u ^ (unsigned)(u >> 32)) * m) >> sh;
+  };
+  for (int bits = 4; (1 << bits) <= DIV_TABLE_SLOTS_MAX; bits++) {
+    if ((size_t)(1 << bits) < 2 * keys.size()) continue;
+    const int sh = 32 - bits;
+    for (unsigned k = 0; k < 4096; k++) {
+      const unsigned m = 0x9E3779B1u + 2u * k * 0x632BE5ABu;  // odd multipliers
+      std::vector<char> used((size_t)1 << bits, 0);
+      bool ok = true;
+      for (uint64_t u : keys) {
+        char& c = used[slot_of(u, m, sh)];
+        if (c) {
+          ok = false;
+          break;
+        }
+        c = 1;
+      }
+      if (!ok) continue;
+      const uint64_t empty = ~0ull;
+      double none;
+      std::memcpy(&none, &empty, 8);
+      tbl.assign((size_t)4 * DIV_TABLE_SLOTS_MAX, none);
+      for (uint64_t u : keys) {
+        double b;
+        std::memcpy(&b, &u, 8);
+        const double yh = 1.0 / b;
+        double* e = &tbl[(size_t)4 * slot_of(u, m, sh)];
+        e[0] = b;
+        e[1] = yh;
+        e[2] = std::fma(-b, yh, 1.0) / b;  // the remainder 1 - b*yh is exact
+        e[3] = 0.0;
+      }
+      *mult = m;
+      *shift = sh;
+      return true;
+    }
+  }
+  return false;
+}
+
 template <class R>
 static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   StepArgs<R> a{};
@@ -219,6 +281,7 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.sp.sdx0 = s0[3];
   a.sp.sdy0 = s0[4];
   a.sp.sdz0 = s0[5];
+  a.dtab = h->dtab;
   a.mat = h->mat;
   a.tab = (const R*)h->tab;
   a.src = h->src;
@@ -288,6 +351,7 @@ static size_t handle_bytes(int nx, int ny, int nz, int precision, int max_steps,
   const int nrec = record_every > 0 ? max_steps / record_every : 0;
   if (nrec > 0) total += r((size_t)nrec * nx * ny * es);
   total += r(sizeof(int) * 2) + r(sizeof(double2) * kEnergyBlocks) + r(sizeof(double) * 2);
+  if (precision == PHONO_F64) total += r(sizeof(double) * 4 * DIV_TABLE_SLOTS_MAX);
   return total;
 }
 
@@ -577,6 +641,18 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   // spacings
   const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
   int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
+  // FP64 leapfrog: divisor table (div_tab in fdtd_step.cu) over the distinct
+  // spacing values and 1.0, the divisors the step uses
+  // (allocated for every FP64 handle, so that phono_footprint is exact)
+  if (f64) {
+    std::vector<double> tbl;
+    double* dt = nullptr;
+    TRY(dalloc(h, (void**)&dt, sizeof(double) * 4 * DIV_TABLE_SLOTS_MAX));
+    if (build_div_table(arrs, lens, tbl, &h->dtab.mult, &h->dtab.shift)) {
+      TRYC(cudaMemcpy(dt, tbl.data(), tbl.size() * sizeof(double), cudaMemcpyHostToDevice));
+      h->dtab.tab = dt;
+    }
+  }
   // device copies carry one value 1 before and two after the array, so the
   // tile pass reads the x spacings of its planes -1..nx without range tests
   // (the padding only reaches values whose results are discarded)
@@ -586,8 +662,12 @@ int phono_create(const phono_desc* d, phono_handle** out) {
     void* spb = nullptr;
     TRY(dalloc(h, &spb, (size_t)(lens[a] + 3) * h->es));
     h->sp[a] = (char*)spb + h->es;
-    TRY(dalloc(h, (void**)&h->sp64[a], (size_t)lens[a] * 8));
-    TRYC(cudaMemcpy(h->sp64[a], arrs[a], (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    TRY(dalloc(h, (void**)&h->rsp64[a], (size_t)lens[a] * 8));
+    {
+      std::vector<double> rec(lens[a]);
+      for (int q = 0; q < lens[a]; q++) rec[q] = 1.0 / arrs[a][q];
+      TRYC(cudaMemcpy(h->rsp64[a], rec.data(), (size_t)lens[a] * 8, cudaMemcpyHostToDevice));
+    }
     if (h->es == 8) {  // F64: raw spacings; F64V: reciprocals in double
       std::vector<double> r(lens[a] + 3, 1.0);
       for (int q = 0; q < lens[a]; q++) r[q + 1] = f64 ? arrs[a][q] : 1.0 / arrs[a][q];
@@ -782,14 +862,15 @@ int phono_energy(phono_handle* h, double out[2]) {
   a.f32 = h->es == 4 ? 1 : 0;
   a.vgiven = f64 ? 0 : 1;
   a.inv_dt = 1.0 / h->d.dt;
-  a.fdx = h->sp64[0];
-  a.fdy = h->sp64[1];
-  a.fdz = h->sp64[2];
-  a.sdx = h->sp64[3];
-  a.sdy = h->sp64[4];
-  a.sdz = h->sp64[5];
+  a.rfdx = h->rsp64[0];
+  a.rfdy = h->rsp64[1];
+  a.rfdz = h->rsp64[2];
+  a.rsdx = h->rsp64[3];
+  a.rsdy = h->rsp64[4];
+  a.rsdz = h->rsp64[5];
   a.mat = h->mat;
   a.tab = h->tab13;
+  a.nmat = h->nmat;
   CK(launch_energy(a, h->partial, kEnergyBlocks, h->energy_out, h->stream));
   CK(cudaMemcpyAsync(out, h->energy_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));

@@ -21,75 +21,93 @@ __device__ __forceinline__ double ld(const void* p, int f32, long long off) {
 }
 
 constexpr int EN_THREADS = 256;
+constexpr int EN_WARPS = EN_THREADS / 32;
 
+// One warp per (i, j) row of the mesh, lanes along k (coalesced loads of every
+// array), rows dealt to the warps of the grid in a fixed order.  Spacings come
+// as FP64 reciprocals (the strain is a difference times 1/spacing) and the
+// material table is staged in shared memory, so a node costs FP64 multiplies
+// and adds only.  Element type T of the displacement / velocity arrays.
+template <class T>
 __global__ void __launch_bounds__(EN_THREADS) energy_partial_kernel(EnergyArgs a, double2* __restrict__ partial) {
+  extern __shared__ double etab[];  // nmat rows of 13
+  for (int q = threadIdx.x; q < a.nmat * 13; q += EN_THREADS) etab[q] = __ldg(a.tab + q);
+  __syncthreads();
   const Geo& g = a.g;
-  const long long n = (long long)g.nx * g.ny * g.nz;
-  double ek = 0.0, es = 0.0;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-    int k = (int)(q % g.nz);
-    long long r = q / g.nz;
-    int j = (int)(r % g.ny);
-    int i = (int)(r / g.ny);
-    long long off = g.o0 + (long long)i * g.sx + (long long)j * g.sy + k;
-    auto rho = [&](int ii, int jj, int kk) {
-      int m = a.mat[g.mo0 + (long long)ii * g.msx + (long long)jj * g.msy + kk];
-      return a.tab[m * 13 + 12];
-    };
-    auto C = [&](int ii, int jj, int kk, int e) {
-      int m = a.mat[g.mo0 + (long long)ii * g.msx + (long long)jj * g.msy + kk];
-      return a.tab[m * 13 + e];
-    };
-    auto U = [&](const void* p, int ii, int jj, int kk) {
-      return ld(p, a.f32, g.o0 + (long long)ii * g.sx + (long long)jj * g.sy + kk);
-    };
-    auto vel = [&](const void* u, const void* v) {
-      double x = ld(v, a.f32, off);
-      return a.vgiven ? x : (ld(u, 0, off) - x) * a.inv_dt;
-    };
-    // kinetic energy at the interior displacement points, absorbing faces excluded
-    if (i <= g.nx - 3 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 2) {
-      double v = vel(a.ux, a.vx);
-      ek += 0.5 * rho(i + 1, j, k) * v * v;
-    }
-    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 3 && k <= g.nz - 2) {
-      double v = vel(a.uy, a.vy);
-      ek += 0.5 * rho(i, j + 1, k) * v * v;
-    }
-    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k <= g.nz - 3) {
-      double v = vel(a.uz, a.vz);
-      ek += 0.5 * rho(i, j, k + 1) * v * v;
-    }
-    // strain energy: normal stresses at interior nodes
-    if (i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
-      double e1 = (U(a.ux, i, j, k) - U(a.ux, i - 1, j, k)) / a.sdx[i - 1];
-      double e2 = (U(a.uy, i, j, k) - U(a.uy, i, j - 1, k)) / a.sdy[j - 1];
-      double e3 = (U(a.uz, i, j, k) - U(a.uz, i, j, k - 1)) / a.sdz[k - 1];
-      double t1 = C(i, j, k, 0) * e1 + C(i, j, k, 1) * e2 + C(i, j, k, 2) * e3;
-      double t2 = C(i, j, k, 3) * e1 + C(i, j, k, 4) * e2 + C(i, j, k, 5) * e3;
-      double t3 = C(i, j, k, 6) * e1 + C(i, j, k, 7) * e2 + C(i, j, k, 8) * e3;
-      es += 0.5 * (t1 * e1 + t2 * e2 + t3 * e3);
-    }
-    // shears at edges
-    if (i >= 1 && i <= g.nx - 2 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
-      double gam = (U(a.uy, i, j, k + 1) - U(a.uy, i, j, k)) / a.fdz[k] +
-                   (U(a.uz, i, j + 1, k) - U(a.uz, i, j, k)) / a.fdy[j];
-      es += 0.5 * C(i, j + 1, k + 1, 9) * gam * gam;
-    }
-    if (i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
-      double gam = (U(a.ux, i, j, k + 1) - U(a.ux, i, j, k)) / a.fdz[k] +
-                   (U(a.uz, i + 1, j, k) - U(a.uz, i, j, k)) / a.fdx[i];
-      es += 0.5 * C(i + 1, j, k + 1, 10) * gam * gam;
-    }
-    if (i <= g.nx - 2 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2) {
-      double gam = (U(a.ux, i, j + 1, k) - U(a.ux, i, j, k)) / a.fdy[j] +
-                   (U(a.uy, i + 1, j, k) - U(a.uy, i, j, k)) / a.fdx[i];
-      es += 0.5 * C(i + 1, j + 1, k, 11) * gam * gam;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * EN_WARPS;
+  const T* ux = (const T*)a.ux;
+  const T* uy = (const T*)a.uy;
+  const T* uz = (const T*)a.uz;
+  const T* vx = (const T*)a.vx;
+  const T* vy = (const T*)a.vy;
+  const T* vz = (const T*)a.vz;
+  const uint8_t* mat = a.mat;
+  double ek = 0.0, es = 0.0;  // sums of rho v^2 and of T . e (the 1/2 is applied once)
+  for (int r = blockIdx.x * EN_WARPS + (threadIdx.x >> 5); r < nx * ny; r += nwarps) {
+    const int i = r / ny, j = r - (r / ny) * ny;
+    const long long o = g.o0 + (long long)i * g.sx + (long long)j * g.sy;      // field (i, j, 0)
+    const long long mo = g.mo0 + (long long)i * g.msx + (long long)j * g.msy;  // material (i, j, 0)
+    // row predicates of the point sets below
+    const bool ix_in = i <= nx - 3, iyz_in = i >= 1 && i <= nx - 2, ish = i <= nx - 2;
+    const bool jx_in = j >= 1 && j <= ny - 2, jy_in = j >= 1 && j <= ny - 3, jsh = j <= ny - 2;
+    const double rsdx = iyz_in ? __ldg(a.rsdx + i - 1) : 0.0, rfdx = ish ? __ldg(a.rfdx + i) : 0.0;
+    const double rsdy = jx_in ? __ldg(a.rsdy + j - 1) : 0.0, rfdy = jsh ? __ldg(a.rfdy + j) : 0.0;
+    for (int k = lane; k < nz; k += 32) {
+      const long long p = o + k;
+      const bool kin = k <= nz - 2, kn = k >= 1 && k <= nz - 2;
+      const double rsdz = kn ? __ldg(a.rsdz + k - 1) : 0.0, rfdz = kn ? __ldg(a.rfdz + k) : 0.0;
+      // kinetic energy at the interior displacement points, absorbing faces excluded
+      auto vel = [&](const T* u, const T* v) {
+        const double x = (double)__ldg(v + p);
+        return a.vgiven ? x : ((double)__ldg(u + p) - x) * a.inv_dt;
+      };
+      if (ix_in && jx_in && kin) {
+        const double v = vel(ux, vx);
+        ek += etab[13 * mat[mo + g.msx + k] + 12] * v * v;
+      }
+      if (iyz_in && jy_in && kin) {
+        const double v = vel(uy, vy);
+        ek += etab[13 * mat[mo + g.msy + k] + 12] * v * v;
+      }
+      if (iyz_in && jx_in && k <= nz - 3) {
+        const double v = vel(uz, vz);
+        ek += etab[13 * mat[mo + k + 1] + 12] * v * v;
+      }
+      if (!kn) continue;  // every strain term below needs 1 <= k <= nz-2
+      // strain energy: normal stresses at interior nodes
+      if (iyz_in && jx_in) {
+        const double* c = etab + 13 * mat[mo + k];
+        const double e1 = ((double)__ldg(ux + p) - (double)__ldg(ux + p - g.sx)) * rsdx;
+        const double e2 = ((double)__ldg(uy + p) - (double)__ldg(uy + p - g.sy)) * rsdy;
+        const double e3 = ((double)__ldg(uz + p) - (double)__ldg(uz + p - 1)) * rsdz;
+        const double t1 = c[0] * e1 + c[1] * e2 + c[2] * e3;
+        const double t2 = c[3] * e1 + c[4] * e2 + c[5] * e3;
+        const double t3 = c[6] * e1 + c[7] * e2 + c[8] * e3;
+        es += t1 * e1 + t2 * e2 + t3 * e3;
+      }
+      // shears at edges
+      if (iyz_in && jsh) {
+        const double gam = ((double)__ldg(uy + p + 1) - (double)__ldg(uy + p)) * rfdz +
+                           ((double)__ldg(uz + p + g.sy) - (double)__ldg(uz + p)) * rfdy;
+        es += etab[13 * mat[mo + g.msy + k + 1] + 9] * gam * gam;
+      }
+      if (ish && jx_in) {
+        const double gam = ((double)__ldg(ux + p + 1) - (double)__ldg(ux + p)) * rfdz +
+                           ((double)__ldg(uz + p + g.sx) - (double)__ldg(uz + p)) * rfdx;
+        es += etab[13 * mat[mo + g.msx + k + 1] + 10] * gam * gam;
+      }
+      if (ish && jsh) {
+        const double gam = ((double)__ldg(ux + p + g.sy) - (double)__ldg(ux + p)) * rfdy +
+                           ((double)__ldg(uy + p + g.sx) - (double)__ldg(uy + p)) * rfdx;
+        es += etab[13 * mat[mo + g.msx + g.msy + k] + 11] * gam * gam;
+      }
     }
   }
   __shared__ double sk[EN_THREADS], ss[EN_THREADS];
-  sk[threadIdx.x] = ek;
-  ss[threadIdx.x] = es;
+  sk[threadIdx.x] = 0.5 * ek;
+  ss[threadIdx.x] = 0.5 * es;
   __syncthreads();
   for (int w = EN_THREADS / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w) {
@@ -127,7 +145,11 @@ __global__ void __launch_bounds__(EN_THREADS) energy_final_kernel(const double2*
 
 // partial must hold nblocks double2 values; out two doubles (device)
 cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st) {
-  energy_partial_kernel<<<nblocks, EN_THREADS, 0, st>>>(a, partial);
+  const size_t smem = (size_t)a.nmat * 13 * sizeof(double);
+  if (a.f32)
+    energy_partial_kernel<float><<<nblocks, EN_THREADS, smem, st>>>(a, partial);
+  else
+    energy_partial_kernel<double><<<nblocks, EN_THREADS, smem, st>>>(a, partial);
   energy_final_kernel<<<1, EN_THREADS, 0, st>>>(partial, nblocks, out);
   return cudaGetLastError();
 }

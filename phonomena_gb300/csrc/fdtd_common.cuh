@@ -66,6 +66,21 @@ struct Spacing {
   R fdx0, fdy0, fdz0, sdx0, sdy0, sdz0;
 };
 
+// Divisor table of the FP64 leapfrog: for each distinct spacing value b of
+// the mesh (and 1.0), entry {b, yh, yl, 0} with yh = RN(1/b) and
+// yl = RN((1 - b*yh)/b), at slot ((lo ^ hi) * mult) >> shift of b's two
+// 32-bit halves (a hash the host picks to be collision-free over the mesh's
+// divisors).  The step divides by b through yh + yl and one remainder
+// correction, which gives the IEEE quotient (div_tab in fdtd_step.cu); a
+// divisor whose slot holds another value takes the IEEE division.
+// tab == nullptr: every division is the IEEE one.
+struct DivTable {
+  const double* tab;  // slots of 4 doubles
+  unsigned mult;
+  int shift;
+};
+constexpr int DIV_TABLE_SLOTS_MAX = 1024;
+
 // Face-point enumeration: for component c and plane p (0 z=N, 1 y=N, 2 y=0,
 // 3 x=N), off[c*4+p] is the first flattened index; off[12] is the total.
 // Planes are disjoint (a point on several faces belongs to the first plane in
@@ -83,6 +98,7 @@ struct StepArgs {
   CUtensorMap tm_pw1;  // own-point tiles of the Kahan terms (velocity forms)
   Geo g;
   Spacing<R> sp;
+  DivTable dtab;
   const uint8_t* __restrict__ mat;
   const R* __restrict__ tab;       // 16 entries per material id
   int nmat;
@@ -132,9 +148,10 @@ struct EnergyArgs {
   int f32;                   // element type of the arrays above (float / double)
   int vgiven;                // vx.. hold the velocity (velocity forms) rather than u_old
   double inv_dt;             // F64: 1/dt to form (u - u_old)/dt
-  const double *fdx, *fdy, *fdz, *sdx, *sdy, *sdz;
+  const double *rfdx, *rfdy, *rfdz, *rsdx, *rsdy, *rsdz;  // reciprocal spacings 1/fd, 1/sd
   const uint8_t* mat;
   const double* tab;  // 13 doubles per material (C..., rho)
+  int nmat;           // rows of tab
 };
 
 }  // namespace phono

@@ -41,27 +41,61 @@ namespace phono {
 // ---------------------------------------------------------------------------
 // arithmetic schemes
 // ---------------------------------------------------------------------------
+// x / b rounded to nearest (the IEEE quotient) from the divisor table entry
+// of b: yh = RN(1/b), yl = RN((1 - b*yh)/b),
+//   q0 = RN(x*yh + RN(x*yl))  is within one ulp of x/b (yh + yl is 1/b to
+//        about 2^-106 relative, and only one rounding of that order follows),
+//   r  = x - q0*b              is then exact (one FMA),
+//   q  = RN(q0 + r*yh)         is RN(x/b) by Markstein's theorem (y within half
+//        an ulp of 1/b, q0 within one ulp of x/b, r exact; P. W. Markstein,
+//        IBM J. Res. Dev. 34(1):111-119, 1990).
+// The argument needs no underflow or overflow on the way, which holds for
+// 2^-800 <= |x| < 2^801 with 2^-40 <= b <= 2^40 (the host enters only such b).
+// Other x (zero, tiny, huge, inf, nan) and divisors without an entry take the
+// IEEE division, except that a zero returns x*yh, the correctly signed zero.
+// One multiply and three FMAs against about a dozen FP64 operations of a
+// general division; the lookup and the range tests are integer work.
+__device__ __forceinline__ double div_tab(double x, double b, const DivTable& d) {
+  const unsigned blo = (unsigned)__double2loint(b), bhi = (unsigned)__double2hiint(b);
+  const unsigned slot = ((blo ^ bhi) * d.mult) >> d.shift;
+  const double2* e = reinterpret_cast<const double2*>(d.tab) + 2 * slot;
+  const double2 e0 = __ldg(e);  // b, yh
+  const double yl = __ldg(reinterpret_cast<const double*>(e + 1));
+  const bool hit = (unsigned)__double2loint(e0.x) == blo && (unsigned)__double2hiint(e0.x) == bhi;
+  const unsigned xhi = (unsigned)__double2hiint(x);
+  const unsigned ex = (xhi >> 20) & 0x7ffu;  // biased exponent of x
+  if (!hit || ex - 223u > 1600u) {
+    const bool zero = ((xhi & 0x7fffffffu) | (unsigned)__double2loint(x)) == 0u;
+    return (hit && zero) ? __dmul_rn(x, e0.y) : __ddiv_rn(x, b);
+  }
+  const double q0 = __fma_rn(x, e0.y, __dmul_rn(x, yl));
+  const double r = __fma_rn(-q0, b, x);
+  return __fma_rn(r, e0.y, q0);
+}
+
 struct F64 {
   using R = double;
   static constexpr bool kahan = false;
   __device__ __forceinline__ static R sub(R a, R b) { return __dsub_rn(a, b); }
+  // x / b with IEEE rounding, through the divisor table when the handle has one
+  __device__ __forceinline__ static R dv(const DivTable& k, R x, R b) { return k.tab ? div_tab(x, b, k) : __ddiv_rn(x, b); }
   // normal stresses ((C0*d1)/a + (C1*d2)/b) + (C2*d3)/d   (base_solver.py:329-351)
-  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
-    return __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(c[0], d1), a), __ddiv_rn(__dmul_rn(c[1], d2), b)),
-                     __ddiv_rn(__dmul_rn(c[2], d3), d));
+  __device__ __forceinline__ static R tn1(const DivTable& k, const R* c, R d1, R d2, R d3, R a, R b, R d) {
+    return __dadd_rn(__dadd_rn(dv(k, __dmul_rn(c[0], d1), a), dv(k, __dmul_rn(c[1], d2), b)),
+                     dv(k, __dmul_rn(c[2], d3), d));
   }
   // shear stress C * (d1/a + d2/b)   (base_solver.py:353-372)
-  __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
-    return __dmul_rn(cs, __dadd_rn(__ddiv_rn(d1, a), __ddiv_rn(d2, b)));
+  __device__ __forceinline__ static R ts(const DivTable& k, R cs, R d1, R a, R d2, R b) {
+    return __dmul_rn(cs, __dadd_rn(dv(k, d1, a), dv(k, d2, b)));
   }
   // (d1/a + d2/b) + d3/c   (base_solver.py:444-446)
-  __device__ __forceinline__ static R div3(R d1, R a, R d2, R b, R d3, R c) {
-    return __dadd_rn(__dadd_rn(__ddiv_rn(d1, a), __ddiv_rn(d2, b)), __ddiv_rn(d3, c));
+  __device__ __forceinline__ static R div3(const DivTable& k, R d1, R a, R d2, R b, R d3, R c) {
+    return __dadd_rn(__dadd_rn(dv(k, d1, a), dv(k, d2, b)), dv(k, d3, c));
   }
   // uz z=0 row as written at base_solver.py:516: ((d1/a + d2/b) + T3[..,1]) - T3[..,0]/fdz
   // with T3[..,0] == +0, so the last subtraction is exact and dropped.
-  __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
-    return __dadd_rn(__dadd_rn(__ddiv_rn(d1, a), __ddiv_rn(d2, b)), t31);
+  __device__ __forceinline__ static R div_surf_ref(const DivTable& k, R d1, R a, R d2, R b, R t31) {
+    return __dadd_rn(__dadd_rn(dv(k, d1, a), dv(k, d2, b)), t31);
   }
   // u[b-+1] + c * (u_new[b-+1] - u[b])   (base_solver.py:540-554)
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
@@ -74,18 +108,18 @@ struct F32K {
   static constexpr bool kahan = true;
   __device__ __forceinline__ static R sub(R a, R b) { return __fsub_rn(a, b); }
   // strains e = d * (1/spacing); T = fmaf(C0, e1, fmaf(C1, e2, C2 * e3))
-  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
+  __device__ __forceinline__ static R tn1(const DivTable&, const R* c, R d1, R d2, R d3, R a, R b, R d) {
     return __fmaf_rn(c[0], __fmul_rn(d1, a), __fmaf_rn(c[1], __fmul_rn(d2, b), __fmul_rn(c[2], __fmul_rn(d3, d))));
   }
-  __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
+  __device__ __forceinline__ static R ts(const DivTable&, R cs, R d1, R a, R d2, R b) {
     return __fmul_rn(cs, __fmaf_rn(d1, a, __fmul_rn(d2, b)));
   }
-  __device__ __forceinline__ static R div3(R d1, R a, R d2, R b, R d3, R c) {
+  __device__ __forceinline__ static R div3(const DivTable&, R d1, R a, R d2, R b, R d3, R c) {
     return __fmaf_rn(d1, a, __fmaf_rn(d2, b, __fmul_rn(d3, c)));
   }
   // reference-precedence z = 0 row: T3[..,1] as the third term with factor 1
-  __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
-    return div3(d1, a, d2, b, t31, 1.0f);
+  __device__ __forceinline__ static R div_surf_ref(const DivTable& k, R d1, R a, R d2, R b, R t31) {
+    return div3(k, d1, a, d2, b, t31, 1.0f);
   }
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __fmaf_rn(coef, __fsub_rn(nbr_new, self_old), nbr_old);
@@ -100,17 +134,17 @@ struct F64V {
   using R = double;
   static constexpr bool kahan = true;
   __device__ __forceinline__ static R sub(R a, R b) { return __dsub_rn(a, b); }
-  __device__ __forceinline__ static R tn1(const R* c, R d1, R d2, R d3, R a, R b, R d) {
+  __device__ __forceinline__ static R tn1(const DivTable&, const R* c, R d1, R d2, R d3, R a, R b, R d) {
     return __fma_rn(c[0], __dmul_rn(d1, a), __fma_rn(c[1], __dmul_rn(d2, b), __dmul_rn(c[2], __dmul_rn(d3, d))));
   }
-  __device__ __forceinline__ static R ts(R cs, R d1, R a, R d2, R b) {
+  __device__ __forceinline__ static R ts(const DivTable&, R cs, R d1, R a, R d2, R b) {
     return __dmul_rn(cs, __fma_rn(d1, a, __dmul_rn(d2, b)));
   }
-  __device__ __forceinline__ static R div3(R d1, R a, R d2, R b, R d3, R c) {
+  __device__ __forceinline__ static R div3(const DivTable&, R d1, R a, R d2, R b, R d3, R c) {
     return __fma_rn(d1, a, __fma_rn(d2, b, __dmul_rn(d3, c)));
   }
-  __device__ __forceinline__ static R div_surf_ref(R d1, R a, R d2, R b, R t31) {
-    return div3(d1, a, d2, b, t31, 1.0);
+  __device__ __forceinline__ static R div_surf_ref(const DivTable& k, R d1, R a, R d2, R b, R t31) {
+    return div3(k, d1, a, d2, b, t31, 1.0);
   }
   __device__ __forceinline__ static R abc(R coef, R nbr_new, R self_old, R nbr_old) {
     return __fma_rn(coef, __dsub_rn(nbr_new, self_old), nbr_old);
@@ -157,8 +191,8 @@ __device__ __forceinline__ typename S::R t1_at(const StepArgs<typename S::R>& a,
   R d1 = S::sub(f.x(i, j, k), f.x(i - 1, j, k));
   R d2 = S::sub(f.y(i, j, k), f.y(i, j - 1, k));
   if (k == 0)  // base_solver.py:408-416: uz - 0, first-element spacings
-    return S::tn1(c, d1, d2, f.z(i, j, 0), a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
-  return S::tn1(c, d1, d2, S::sub(f.z(i, j, k), f.z(i, j, k - 1)), __ldg(a.sp.sdx + i - 1),
+    return S::tn1(a.dtab, c, d1, d2, f.z(i, j, 0), a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+  return S::tn1(a.dtab, c, d1, d2, S::sub(f.z(i, j, k), f.z(i, j, k - 1)), __ldg(a.sp.sdx + i - 1),
                 __ldg(a.sp.sdy + j - 1), __ldg(a.sp.sdz + k - 1));
 }
 
@@ -176,15 +210,15 @@ __device__ __forceinline__ void t123_at(const StepArgs<typename S::R>& a, const 
   R d2 = S::sub(f.y(i, j, k), f.y(i, j - 1, k));
   if (k == 0) {
     R d3 = f.z(i, j, 0);
-    T1 = S::tn1(c, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
-    T2 = S::tn1(c + 3, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+    T1 = S::tn1(a.dtab, c, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
+    T2 = S::tn1(a.dtab, c + 3, d1, d2, d3, a.sp.sdx0, a.sp.sdy0, a.sp.sdz0);
     T3 = R(0);
   } else {
     R d3 = S::sub(f.z(i, j, k), f.z(i, j, k - 1));
     R sa = __ldg(a.sp.sdx + i - 1), sb = __ldg(a.sp.sdy + j - 1), sd = __ldg(a.sp.sdz + k - 1);
-    T1 = S::tn1(c, d1, d2, d3, sa, sb, sd);
-    T2 = S::tn1(c + 3, d1, d2, d3, sa, sb, sd);
-    T3 = S::tn1(c + 6, d1, d2, d3, sa, sb, sd);
+    T1 = S::tn1(a.dtab, c, d1, d2, d3, sa, sb, sd);
+    T2 = S::tn1(a.dtab, c + 3, d1, d2, d3, sa, sb, sd);
+    T3 = S::tn1(a.dtab, c + 6, d1, d2, d3, sa, sb, sd);
   }
 }
 
@@ -194,9 +228,9 @@ __device__ __forceinline__ typename S::R t4_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 1 || i > g.nx - 2 || j < 0 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:420-423
-    return S::ts(f.row(i, j + 1, 0)[9], S::sub(f.y(i, j, 1), f.y(i, j, 0)), a.sp.fdy0,
+    return S::ts(a.dtab, f.row(i, j + 1, 0)[9], S::sub(f.y(i, j, 1), f.y(i, j, 0)), a.sp.fdy0,
                  S::sub(f.z(i, j + 1, 0), f.z(i, j, 0)), a.sp.fdz0);
-  return S::ts(f.row(i, j + 1, k + 1)[9], S::sub(f.y(i, j, k + 1), f.y(i, j, k)), __ldg(a.sp.fdz + k),
+  return S::ts(a.dtab, f.row(i, j + 1, k + 1)[9], S::sub(f.y(i, j, k + 1), f.y(i, j, k)), __ldg(a.sp.fdz + k),
                S::sub(f.z(i, j + 1, k), f.z(i, j, k)), __ldg(a.sp.fdy + j));
 }
 
@@ -206,9 +240,9 @@ __device__ __forceinline__ typename S::R t5_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 0 || i > g.nx - 2 || j < 1 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:425-428
-    return S::ts(f.row(i + 1, j, 0)[10], S::sub(f.x(i, j, 1), f.x(i, j, 0)), a.sp.fdx0,
+    return S::ts(a.dtab, f.row(i + 1, j, 0)[10], S::sub(f.x(i, j, 1), f.x(i, j, 0)), a.sp.fdx0,
                  S::sub(f.z(i + 1, j, 0), f.z(i, j, 0)), a.sp.fdz0);
-  return S::ts(f.row(i + 1, j, k + 1)[10], S::sub(f.x(i, j, k + 1), f.x(i, j, k)), __ldg(a.sp.fdz + k),
+  return S::ts(a.dtab, f.row(i + 1, j, k + 1)[10], S::sub(f.x(i, j, k + 1), f.x(i, j, k)), __ldg(a.sp.fdz + k),
                S::sub(f.z(i + 1, j, k), f.z(i, j, k)), __ldg(a.sp.fdx + i));
 }
 
@@ -218,9 +252,9 @@ __device__ __forceinline__ typename S::R t6_at(const StepArgs<typename S::R>& a,
   const Geo& g = a.g;
   if (i < 0 || i > g.nx - 2 || j < 0 || j > g.ny - 2 || k < 0 || k > g.nz - 2) return R(0);
   if (k == 0)  // base_solver.py:430-433
-    return S::ts(f.row(i + 1, j + 1, 0)[11], S::sub(f.x(i, j + 1, 0), f.x(i, j, 0)), a.sp.fdx0,
+    return S::ts(a.dtab, f.row(i + 1, j + 1, 0)[11], S::sub(f.x(i, j + 1, 0), f.x(i, j, 0)), a.sp.fdx0,
                  S::sub(f.y(i + 1, j, 0), f.y(i, j, 0)), a.sp.fdz0);
-  return S::ts(f.row(i + 1, j + 1, k)[11], S::sub(f.x(i, j + 1, k), f.x(i, j, k)), __ldg(a.sp.fdy + j),
+  return S::ts(a.dtab, f.row(i + 1, j + 1, k)[11], S::sub(f.x(i, j + 1, k), f.x(i, j, k)), __ldg(a.sp.fdy + j),
                S::sub(f.y(i + 1, j, k), f.y(i, j, k)), __ldg(a.sp.fdx + i));
 }
 
@@ -233,10 +267,10 @@ __device__ __forceinline__ typename S::R div_x(const StepArgs<typename S::R>& a,
                                                const typename S::R*& row) {
   if (k == 0) {
     row = f.row(i + 1, j, 0);
-    return S::div3(S::sub(t1p, t1m), a.sp.fdx0, S::sub(t6a, t6b), a.sp.sdy0, t5a, a.sp.sdz0);
+    return S::div3(a.dtab, S::sub(t1p, t1m), a.sp.fdx0, S::sub(t6a, t6b), a.sp.sdy0, t5a, a.sp.sdz0);
   }
   row = f.row(i + 1, j, k);
-  return S::div3(S::sub(t1p, t1m), __ldg(a.sp.fdx + i), S::sub(t6a, t6b), __ldg(a.sp.sdy + j - 1),
+  return S::div3(a.dtab, S::sub(t1p, t1m), __ldg(a.sp.fdx + i), S::sub(t6a, t6b), __ldg(a.sp.sdy + j - 1),
                  S::sub(t5a, t5b), __ldg(a.sp.sdz + k - 1));
 }
 template <class S, class F>
@@ -246,10 +280,10 @@ __device__ __forceinline__ typename S::R div_y(const StepArgs<typename S::R>& a,
                                                const typename S::R*& row) {
   if (k == 0) {
     row = f.row(i, j + 1, 0);
-    return S::div3(S::sub(t6a, t6b), a.sp.sdx0, S::sub(t2p, t2m), a.sp.fdy0, t4a, a.sp.sdz0);
+    return S::div3(a.dtab, S::sub(t6a, t6b), a.sp.sdx0, S::sub(t2p, t2m), a.sp.fdy0, t4a, a.sp.sdz0);
   }
   row = f.row(i, j + 1, k);
-  return S::div3(S::sub(t6a, t6b), __ldg(a.sp.sdx + i - 1), S::sub(t2p, t2m), __ldg(a.sp.fdy + j),
+  return S::div3(a.dtab, S::sub(t6a, t6b), __ldg(a.sp.sdx + i - 1), S::sub(t2p, t2m), __ldg(a.sp.fdy + j),
                  S::sub(t4a, t4b), __ldg(a.sp.sdz + k - 1));
 }
 template <class S, class F>
@@ -259,11 +293,11 @@ __device__ __forceinline__ typename S::R div_z(const StepArgs<typename S::R>& a,
                                                const typename S::R*& row) {
   if (k == 0) {
     row = f.row(i, j, 0);  // density at z index 0 (base_solver.py:513)
-    if (a.surface_mode == 0) return S::div_surf_ref(S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p);
-    return S::div3(S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p, a.sp.fdz0);
+    if (a.surface_mode == 0) return S::div_surf_ref(a.dtab, S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p);
+    return S::div3(a.dtab, S::sub(t5a, t5b), a.sp.sdx0, S::sub(t4a, t4b), a.sp.sdy0, t3p, a.sp.fdz0);
   }
   row = f.row(i, j, k + 1);
-  return S::div3(S::sub(t5a, t5b), __ldg(a.sp.sdx + i - 1), S::sub(t4a, t4b), __ldg(a.sp.sdy + j - 1),
+  return S::div3(a.dtab, S::sub(t5a, t5b), __ldg(a.sp.sdx + i - 1), S::sub(t4a, t4b), __ldg(a.sp.sdy + j - 1),
                  S::sub(t3p, t3m), __ldg(a.sp.fdz + k));
 }
 

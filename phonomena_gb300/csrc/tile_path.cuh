@@ -151,14 +151,14 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
     const R c = tab[16 * Mp[Lm + dm + (kzero ? 0 : 1)] + 10];
     const R d1 = S::sub(U0[XO + Lu + du + 1], U0[XO + Lu + du]);
     const R d2 = S::sub(Up[ZO + Lu + du], U0[ZO + Lu + du]);
-    return S::ts(c, d1, kzero ? a.sp.fdx0 : fz, d2, kzero ? a.sp.fdz0 : fx);
+    return S::ts(a.dtab, c, d1, kzero ? a.sp.fdx0 : fz, d2, kzero ? a.sp.fdz0 : fx);
   };
   // T6 (base_solver.py:367-372, 430-433)
   auto T6f = [&](const R* U0, const R* Up, const uint8_t* Mp, int du, int dm, bool kzero, R fy, R fx) {
     const R c = tab[16 * Mp[Lm + dm + MKW] + 11];
     const R d1 = S::sub(U0[XO + Lu + du + KW], U0[XO + Lu + du]);
     const R d2 = S::sub(Up[YO + Lu + du], U0[YO + Lu + du]);
-    return S::ts(c, d1, kzero ? a.sp.fdx0 : fy, d2, kzero ? a.sp.fdz0 : fx);
+    return S::ts(a.dtab, c, d1, kzero ? a.sp.fdx0 : fy, d2, kzero ? a.sp.fdz0 : fx);
   };
 
   // Halo stresses the neighbours need: T2 row j0+TJ, T6 / T4 row j0-1, T3
@@ -326,28 +326,28 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
       const R d2 = S::sub(uyc, U0[YO + Lu - KW]);
       const R d3 = S::sub(uzc, U0[ZO + Lu - 1]);
       const R sa = kz ? a.sp.sdx0 : sdx_im;
-      t1c = S::tn1(cc, d1, d2, d3, sa, t123_b, t123_d);
-      t2c = S::tn1(cc + 3, d1, d2, d3, sa, t123_b, t123_d);
-      if (!kz) t3c = S::tn1(cc + 6, d1, d2, d3, sa, t123_b, t123_d);  // T3[1:-1,1:-1,0] = 0 (:418)
+      t1c = S::tn1(a.dtab, cc, d1, d2, d3, sa, t123_b, t123_d);
+      t2c = S::tn1(a.dtab, cc + 3, d1, d2, d3, sa, t123_b, t123_d);
+      if (!kz) t3c = S::tn1(a.dtab, cc + 6, d1, d2, d3, sa, t123_b, t123_d);  // T3[1:-1,1:-1,0] = 0 (:418)
     }
     R t4c = R(0), t5c = R(0), t6c = R(0);
     if (i_n && j_s && k_in) {  // T4 (base_solver.py:353-358, 420-423)
       const R c = tab[16 * (kz ? id_y : (int)M0[Lm + MKW + 1]) + 9];
       const R d1 = S::sub(U0[YO + Lu + 1], uyc);
       const R d2 = S::sub(U0[ZO + Lu + KW], uzc);
-      t4c = S::ts(c, d1, kz ? a.sp.fdy0 : fdz_k, d2, kz ? a.sp.fdz0 : fdy_j);
+      t4c = S::ts(a.dtab, c, d1, kz ? a.sp.fdy0 : fdz_k, d2, kz ? a.sp.fdz0 : fdy_j);
     }
     if (i_s && j_n && k_in) {  // T5 (base_solver.py:360-365, 425-428)
       const R c = tab[16 * (kz ? idp_c : idp_z) + 10];
       const R d1 = S::sub(uxc_up, uxc);
       const R d2 = S::sub(uzc_n, uzc);
-      t5c = S::ts(c, d1, kz ? a.sp.fdx0 : fdz_k, d2, kz ? a.sp.fdz0 : fdx_i);
+      t5c = S::ts(a.dtab, c, d1, kz ? a.sp.fdx0 : fdz_k, d2, kz ? a.sp.fdz0 : fdx_i);
     }
     if (i_s && j_s && k_in) {  // T6 (base_solver.py:367-372, 430-433)
       const R c = tab[16 * idp_y + 11];
       const R d1 = S::sub(U0[XO + Lu + KW], uxc);
       const R d2 = S::sub(uyc_n, uyc);
-      t6c = S::ts(c, d1, kz ? a.sp.fdx0 : fdy_j, d2, kz ? a.sp.fdz0 : fdx_i);
+      t6c = S::ts(a.dtab, c, d1, kz ? a.sp.fdx0 : fdy_j, d2, kz ? a.sp.fdz0 : fdx_i);
     }
     sT2[L] = t2c;
     sT3[L] = t3c;
@@ -363,7 +363,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           const R d1 = S::sub(U0[XO + h_u], Um[XO + h_u]);
           const R d2 = S::sub(U0[YO + h_u], U0[YO + h_u - KW]);
           const R d3 = S::sub(U0[ZO + h_u], U0[ZO + h_u - 1]);
-          v = S::tn1(c, d1, d2, d3, h_z0 ? a.sp.sdx0 : sdx_im, h_a, h_b);
+          v = S::tn1(a.dtab, c, d1, d2, d3, h_z0 ? a.sp.sdx0 : sdx_im, h_a, h_b);
         }
         (h_which == 1 ? sT2 : sT3)[h_dst] = v;
       } else if (hk == 1) {  // T6 row below
@@ -371,7 +371,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           const R c = tab[16 * Mp[h_m] + 11];
           const R d1 = S::sub(U0[XO + h_u + KW], U0[XO + h_u]);
           const R d2 = S::sub(Up[YO + h_u], U0[YO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
         }
         sT6[p * PL + h_dst] = v;
       } else if (hk == 2) {  // T4 row below / column left
@@ -379,7 +379,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           const R c = tab[16 * M0[h_m] + 9];
           const R d1 = S::sub(U0[YO + h_u + 1], U0[YO + h_u]);
           const R d2 = S::sub(U0[ZO + h_u + KW], U0[ZO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_b);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_b);
         }
         sT4[h_dst] = v;
       } else {  // T5 column left
@@ -387,7 +387,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           const R c = tab[16 * Mp[h_m] + 10];
           const R d1 = S::sub(U0[XO + h_u + 1], U0[XO + h_u]);
           const R d2 = S::sub(Up[ZO + h_u], U0[ZO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
         }
         sT5[p * PL + h_dst] = v;
       }
@@ -413,7 +413,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           if (i_n) {
             // at k = 0 the T4(k-1) halo entry is 0, so T4 - 0 is the z = 0 row's "T4 - 0"
             const R* row = tab + 16 * id_y;
-            const R dv = S::div3(S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
+            const R dv = S::div3(a.dtab, S::sub(t6c, t6m), kz ? a.sp.sdx0 : sdx_im, S::sub(sT2[L + W], t2c), uy_b,
                                  S::sub(t4c, sT4[L - 1]), uy_c);
             R vn, cn;
             val = update_value<S>(uyc, Pw<R>{PW0[P::PWC], S::kahan ? PW0[4 * P::PWC] : R(0)}, dv, row[12], a.dt, vn,
@@ -432,7 +432,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
             // z = 0 row: density at z index 0 (base_solver.py:513); T3(k) = 0 there,
             // and the reference precedence (:516) adds T3[..,1] with factor 1
             const R* row = tab + 16 * (kz ? id_c : id_z);
-            const R dv = S::div3(S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
+            const R dv = S::div3(a.dtab, S::sub(t5c, t5m), kz ? a.sp.sdx0 : sdx_im, S::sub(t4c, sT4[L - W]), uz_b,
                                  S::sub(sT3[L + 1], t3c), uz_c);
             R vn, cn;
             val = update_value<S>(uzc, Pw<R>{PW0[2 * P::PWC], S::kahan ? PW0[5 * P::PWC] : R(0)}, dv, row[12], a.dt,
@@ -457,7 +457,7 @@ __device__ __forceinline__ bool tile_block(const StepArgs<typename S::R>& a, uns
           const int pm = p ^ 1;
           const R* row = tab + 16 * id_c;  // P[(i-1)+1, j, k]
           // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
-          const R dv = S::div3(S::sub(t1c, t1m), kz ? a.sp.fdx0 : fdx_im,
+          const R dv = S::div3(a.dtab, S::sub(t1c, t1m), kz ? a.sp.fdx0 : fdx_im,
                                S::sub(sT6[pm * PL + L], sT6[pm * PL + L - W]), ux_b,
                                S::sub(sT5[pm * PL + L], sT5[pm * PL + L - 1]), ux_c);
           R vn, cn;

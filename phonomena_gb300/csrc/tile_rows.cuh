@@ -257,12 +257,12 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
       t6m[q] = R(0);
       if (i_s && j_n[q] && k_in) {  // T5 (base_solver.py:360-365, 425-428)
         const R c = tab[16 * Mp[lm + (kz ? 0 : 1)] + 10];
-        t5m[q] = S::ts(c, S::sub(U0[XO + lu + 1], U0[XO + lu]), kz ? a.sp.fdx0 : fdz_k,
+        t5m[q] = S::ts(a.dtab, c, S::sub(U0[XO + lu + 1], U0[XO + lu]), kz ? a.sp.fdx0 : fdz_k,
                        S::sub(Up[ZO + lu], U0[ZO + lu]), kz ? a.sp.fdz0 : fx);
       }
       if (i_s && j_s[q] && k_in) {  // T6 (base_solver.py:367-372, 430-433)
         const R c = tab[16 * Mp[lm + MKW] + 11];
-        t6m[q] = S::ts(c, S::sub(U0[XO + lu + KW], U0[XO + lu]), kz ? a.sp.fdx0 : fdy_j[q],
+        t6m[q] = S::ts(a.dtab, c, S::sub(U0[XO + lu + KW], U0[XO + lu]), kz ? a.sp.fdx0 : fdy_j[q],
                        S::sub(Up[YO + lu], U0[YO + lu]), kz ? a.sp.fdz0 : fx);
       }
       t1m[q] = R(0);
@@ -345,28 +345,28 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
         const R d1 = S::sub(uxc[q], uxm[q]);
         const R d2 = S::sub(uyc[q], U0[YO + lu - KW]);
         const R d3 = S::sub(uzc[q], U0[ZO + lu - 1]);
-        t1c[q] = S::tn1(cc, d1, d2, d3, SA, sb[q], t123_d);
-        t2c[q] = S::tn1(cc + 3, d1, d2, d3, SA, sb[q], t123_d);
-        if (!kz) t3c[q] = S::tn1(cc + 6, d1, d2, d3, SA, sb[q], t123_d);  // T3[1:-1,1:-1,0] = 0 (:418)
+        t1c[q] = S::tn1(a.dtab, cc, d1, d2, d3, SA, sb[q], t123_d);
+        t2c[q] = S::tn1(a.dtab, cc + 3, d1, d2, d3, SA, sb[q], t123_d);
+        if (!kz) t3c[q] = S::tn1(a.dtab, cc + 6, d1, d2, d3, SA, sb[q], t123_d);  // T3[1:-1,1:-1,0] = 0 (:418)
       }
       t4c[q] = t5c[q] = t6c[q] = R(0);
       if (i_n && j_s[q] && k_in) {  // T4 (base_solver.py:353-358, 420-423)
         const R c = tab[16 * (kz ? id_y[q] : (int)M0[lm + MKW + 1]) + 9];
         const R d1 = S::sub(U0[YO + lu + 1], uyc[q]);
         const R d2 = S::sub(U0[ZO + lu + KW], uzc[q]);
-        t4c[q] = S::ts(c, d1, kz ? a.sp.fdy0 : fdz_k, d2, kz ? a.sp.fdz0 : fdy_j[q]);
+        t4c[q] = S::ts(a.dtab, c, d1, kz ? a.sp.fdy0 : fdz_k, d2, kz ? a.sp.fdz0 : fdy_j[q]);
       }
       if (i_s && j_n[q] && k_in) {  // T5 (base_solver.py:360-365, 425-428)
         const R c = tab[16 * (kz ? idp_c[q] : idp_z[q]) + 10];
         const R d1 = S::sub(uxc_up[q], uxc[q]);
         const R d2 = S::sub(uzc_n[q], uzc[q]);
-        t5c[q] = S::ts(c, d1, kz ? a.sp.fdx0 : fdz_k, d2, SX5);
+        t5c[q] = S::ts(a.dtab, c, d1, kz ? a.sp.fdx0 : fdz_k, d2, SX5);
       }
       if (i_s && j_s[q] && k_in) {  // T6 (base_solver.py:367-372, 430-433)
         const R c = tab[16 * idp_y[q] + 11];
         const R d1 = S::sub(U0[XO + lu + KW], uxc[q]);
         const R d2 = S::sub(uyc_n[q], uyc[q]);
-        t6c[q] = S::ts(c, d1, kz ? a.sp.fdx0 : fdy_j[q], d2, SX5);
+        t6c[q] = S::ts(a.dtab, c, d1, kz ? a.sp.fdx0 : fdy_j[q], d2, SX5);
       }
       const int l = L + q * W;
       sT2[l] = t2c[q];
@@ -384,7 +384,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           const R d1 = S::sub(U0[XO + h_u], Um[XO + h_u]);
           const R d2 = S::sub(U0[YO + h_u], U0[YO + h_u - KW]);
           const R d3 = S::sub(U0[ZO + h_u], U0[ZO + h_u - 1]);
-          v = S::tn1(c, d1, d2, d3, h_z0 ? a.sp.sdx0 : sdx_im, h_a, h_b);
+          v = S::tn1(a.dtab, c, d1, d2, d3, h_z0 ? a.sp.sdx0 : sdx_im, h_a, h_b);
         }
         (h_which == 1 ? sT2 : sT3)[h_dst] = v;
       } else if (hk == 1) {  // T6 row below
@@ -392,7 +392,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           const R c = tab[16 * Mp[h_m] + 11];
           const R d1 = S::sub(U0[XO + h_u + KW], U0[XO + h_u]);
           const R d2 = S::sub(Up[YO + h_u], U0[YO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
         }
         sT6[p * PL + h_dst] = v;
       } else if (hk == 2) {  // T4 row below / column left
@@ -400,7 +400,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           const R c = tab[16 * M0[h_m] + 9];
           const R d1 = S::sub(U0[YO + h_u + 1], U0[YO + h_u]);
           const R d2 = S::sub(U0[ZO + h_u + KW], U0[ZO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_b);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_b);
         }
         sT4[h_dst] = v;
       } else {  // T5 column left
@@ -408,7 +408,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           const R c = tab[16 * Mp[h_m] + 10];
           const R d1 = S::sub(U0[XO + h_u + 1], U0[XO + h_u]);
           const R d2 = S::sub(Up[ZO + h_u], U0[ZO + h_u]);
-          v = S::ts(c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
+          v = S::ts(a.dtab, c, d1, h_a, d2, h_z0 ? a.sp.fdz0 : fdx_i);
         }
         sT5[p * PL + h_dst] = v;
       }
@@ -440,7 +440,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           if (i_n) {
             // at k = 0 the T4(k-1) halo entry is 0, so T4 - 0 is the z = 0 row's "T4 - 0"
             const R* row = tab + 16 * id_y[q];
-            const R dv = S::div3(S::sub(t6c[q], t6m[q]), SA, S::sub(sT2[l + W], t2c[q]), uy_b[q],
+            const R dv = S::div3(a.dtab, S::sub(t6c[q], t6m[q]), SA, S::sub(sT2[l + W], t2c[q]), uy_b[q],
                                  S::sub(t4c[q], sT4[l - 1]), t123_d);
             R vn, cn;
             val = update_value<S>(uyc[q], Pw<R>{PW0[P::PWC + q * TK], S::kahan ? PW0[4 * P::PWC + q * TK] : R(0)},
@@ -459,7 +459,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
             // z = 0 row: density at z index 0 (base_solver.py:513); T3(k) = 0 there,
             // and the reference precedence (:516) adds T3[..,1] with factor 1
             const R* row = tab + 16 * (kz ? id_c[q] : id_z[q]);
-            const R dv = S::div3(S::sub(t5c[q], t5m[q]), SA, S::sub(t4c[q], sT4[l - W]), sb[q],
+            const R dv = S::div3(a.dtab, S::sub(t5c[q], t5m[q]), SA, S::sub(t4c[q], sT4[l - W]), sb[q],
                                  S::sub(sT3[l + 1], t3c[q]), uz_c);
             R vn, cn;
             val = update_value<S>(uzc[q],
@@ -484,7 +484,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
         if (j_n[q]) {
           const R* row = tab + 16 * id_c[q];  // P[(i-1)+1, j, k]
           // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
-          const R dv = S::div3(S::sub(t1c[q], t1m[q]), kz ? a.sp.fdx0 : fdx_im,
+          const R dv = S::div3(a.dtab, S::sub(t1c[q], t1m[q]), kz ? a.sp.fdx0 : fdx_im,
                                S::sub(sT6[pm * PL + l], sT6[pm * PL + l - W]), sb[q],
                                S::sub(sT5[pm * PL + l], sT5[pm * PL + l - 1]), t123_d);
           R vn, cn;

@@ -124,6 +124,24 @@ def test_f64_and_f32k_vs_oracle_multi_tile(gpu_lib, oracle, cells, tile_j):
         assert np.array_equal(sim.read_surface(), surf32)
 
 
+def test_f64_without_divisor_table_vs_oracle(gpu_lib, oracle):
+    """A mesh with more distinct spacings than the divisor table takes (random
+    non-uniform x spacings) divides with IEEE division everywhere; the result
+    is the oracle's bit for bit."""
+    d = _crystal_case((640, 6, 5), 30, seed=5)
+    rng = np.random.default_rng(5)
+    fdx = d["fdx"] * rng.uniform(0.95, 1.25, d["fdx"].shape)
+    d["fdx"], d["sdx"] = fdx, (fdx[1:] + fdx[:-1]) / 2.0
+    assert len(np.unique(np.concatenate([d[k] for k in ("fdx", "sdx")]))) > 1024
+    s64, surf64 = oracle.run_f64(_oracle_prob(oracle, d), record_every=10)
+    with device_sim(d) as sim:
+        sim.step(30)
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), s64.u):
+            assert np.array_equal(sim.download(key), ref), key
+        assert np.array_equal(sim.read_surface(), surf64)
+
+
 def test_f64v_matches_reference_arithmetic(gpu_lib):
     """The FP64 velocity form (the fast FP64 error reference) agrees with the
     reference-arithmetic FP64 path to 1e-12 relative L2 over 500 steps."""
@@ -176,23 +194,57 @@ def test_upload_download_resume(gpu_lib):
             assert G.matches(d, key, b.download(key))
 
 
-def test_energy_matches_numpy(gpu_lib):
+def _energy_numpy(d, u, vel):
+    """Kinetic and strain energy restated in numpy: 1/2 rho v^2 over the
+    interior displacement points, 1/2 T . e over the reference's normal-stress
+    nodes and shear edges (base_solver.py:329-372)."""
+    ux, uy, uz = u
+    ids, tab = d["ids"], d["table"]
+    nx, ny, nz = ids.shape
+    rho = tab[ids, 12]
+    vx, vy, vz = vel
+    ek = 0.5 * (np.sum(rho[1:-1, 1:-1, :-1] * vx[:-1, 1:-1, :-1] ** 2)
+                + np.sum(rho[1:-1, 2:-1, :-1] * vy[1:-1, 1:-1, :-1] ** 2)
+                + np.sum(rho[1:-1, 1:-1, 1:-1] * vz[1:-1, 1:-1, :-1] ** 2))
+    fdx, fdy, fdz = d["fdx"], d["fdy"], d["fdz"]
+    sdx, sdy, sdz = d["sdx"], d["sdy"], d["sdz"]
+    I, J, K = slice(1, nx - 1), slice(1, ny - 1), slice(1, nz - 1)
+    e1 = (ux[1:nx - 1, J, K] - ux[0:nx - 2, J, K]) / sdx[:, None, None]
+    e2 = (uy[I, 1:ny - 1, K] - uy[I, 0:ny - 2, K]) / sdy[None, :, None]
+    e3 = (uz[I, J, 1:nz - 1] - uz[I, J, 0:nz - 2]) / sdz[None, None, :]
+    c = tab[ids[I, J, K]]
+    t1 = c[..., 0] * e1 + c[..., 1] * e2 + c[..., 2] * e3
+    t2 = c[..., 3] * e1 + c[..., 4] * e2 + c[..., 5] * e3
+    t3 = c[..., 6] * e1 + c[..., 7] * e2 + c[..., 8] * e3
+    es = 0.5 * np.sum(t1 * e1 + t2 * e2 + t3 * e3)
+    g4 = ((uy[I, 0:ny - 1, 2:nz] - uy[I, 0:ny - 1, 1:nz - 1]) / fdz[None, None, 1:]
+          + (uz[I, 1:ny, 1:nz - 1] - uz[I, 0:ny - 1, 1:nz - 1]) / fdy[None, :, None])
+    g5 = ((ux[0:nx - 1, J, 2:nz] - ux[0:nx - 1, J, 1:nz - 1]) / fdz[None, None, 1:]
+          + (uz[1:nx, J, 1:nz - 1] - uz[0:nx - 1, J, 1:nz - 1]) / fdx[:, None, None])
+    g6 = ((ux[0:nx - 1, 1:ny, K] - ux[0:nx - 1, 0:ny - 1, K]) / fdy[None, :, None]
+          + (uy[1:nx, 0:ny - 1, K] - uy[0:nx - 1, 0:ny - 1, K]) / fdx[:, None, None])
+    es += 0.5 * (np.sum(tab[ids[I, 1:ny, 2:nz], 9] * g4 ** 2) + np.sum(tab[ids[1:nx, J, 2:nz], 10] * g5 ** 2)
+                 + np.sum(tab[ids[1:nx, 1:ny, K], 11] * g6 ** 2))
+    return ek, es
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32k"])
+def test_energy_matches_numpy(gpu_lib, precision):
     d = G.load("small3_corrected")
-    with device_sim(d) as sim:
+    with device_sim(d, precision=precision) as sim:
         sim.step(d["meta"]["steps"])
         sim.sync()
         ek, es = sim.energy()
-        ux, uy, uz = (sim.download(k) for k in ("ux", "uy", "uz"))
-        ox, oy, oz = (sim.download(k) for k in ("ux_old", "uy_old", "uz_old"))
-    nx, ny, nz = d["ids"].shape
-    rho = d["table"][d["ids"], 12]
-    dt = d["dt"]
-    # interior points without the absorbing faces
-    ek_ref = 0.5 * (np.sum(rho[1:-1, 1:-1, :-1] * ((ux - ox)[:-1, 1:-1, :-1] / dt) ** 2)
-                    + np.sum(rho[1:-1, 2:-1, :-1] * ((uy - oy)[1:-1, 1:-1, :-1] / dt) ** 2)
-                    + np.sum(rho[1:-1, 1:-1, 1:-1] * ((uz - oz)[1:-1, 1:-1, :-1] / dt) ** 2))
-    assert abs(ek - ek_ref) <= 1e-9 * abs(ek_ref)
-    assert es > 0
+        u = [sim.download(k).astype(np.float64) for k in ("ux", "uy", "uz")]
+        if precision == "f64":
+            old = [sim.download(k) for k in ("ux_old", "uy_old", "uz_old")]
+            vel = [(a - b) / d["dt"] for a, b in zip(u, old)]
+        else:
+            vel = [sim.download(k).astype(np.float64) for k in ("vx", "vy", "vz")]
+    ek_ref, es_ref = _energy_numpy(d, u, vel)
+    assert ek_ref > 0 and es_ref > 0
+    assert abs(ek - ek_ref) <= 1e-9 * abs(ek_ref), (ek, ek_ref)
+    assert abs(es - es_ref) <= 1e-9 * abs(es_ref), (es, es_ref)
 
 
 def test_numeric_guard_reports_nonfinite(gpu_lib):
