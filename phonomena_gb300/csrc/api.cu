@@ -200,12 +200,55 @@ static int upload_table(phono_handle* h, const double* table, int nmat, int id00
   return PHONO_OK;
 }
 
-// Divisor table of the FP64 leapfrog: one slot of {b, RN(1/b), RN((1-b*yh)/b), 0}
-// per distinct divisor b (every spacing value in [2^-40, 2^40], and 1.0), at
-// slot ((lo ^ hi) * mult) >> shift of b's 32-bit halves; mult and the slot
-// count are searched until no two divisors share a slot.  Empty slots hold a
-// bit pattern no divisor has, so they never match.  false: no table (too many
-// distinct values), every division stays the IEEE one.
+// Whether q0 = RN(x*yh + RN(x*yl)) is the IEEE quotient x/b for every x (no
+// underflow or overflow).  q0 is off x/b by less than 2^-105 relative, so it
+// can round the wrong way only where x/b lies that close to a rounding
+// midpoint mu.  With b = H * 2^e (H odd) and mu = M * 2^f (M odd, 54 bits),
+// x = X * 2^g is that close exactly when H*M = X * 2^D + c with a small
+// integer c (|c| <= 4 follows from the bound; 8 are tried) and D the
+// alignment of X against H*M: M = c * H^-1 mod 2^D.  Every such x (up to a
+// power of two, which scales the quotient exactly) is tried here.  Approach
+// of Brisebarre, Muller and Raina (IEEE Trans. Computers 54(7), 2005).
+static bool two_op_exact(double b, double yh, double yl) {
+  uint64_t hb;
+  std::memcpy(&hb, &b, 8);
+  int eh = (int)((hb >> 52) & 0x7ff) - 1075;
+  uint64_t H = (hb & ((1ull << 52) - 1)) | (1ull << 52);
+  while (!(H & 1)) {
+    H >>= 1;
+    eh++;
+  }
+  uint64_t inv = H;  // H^-1 mod 2^64 by Newton iteration
+  for (int q = 0; q < 6; q++) inv *= 2 - H * inv;
+  for (int D = 50; D <= 54; D++) {
+    const uint64_t mask = (1ull << D) - 1;
+    for (int c = -8; c <= 8; c++) {
+      if (c == 0) continue;
+      for (uint64_t M = ((uint64_t)(int64_t)c * inv) & mask; M < (1ull << 54); M += 1ull << D) {
+        if (M >= (1ull << 53) && (M & 1)) {
+          const unsigned __int128 Xc = (unsigned __int128)H * M - (unsigned __int128)(__int128)c;
+          if ((uint64_t)(Xc & mask) == 0) {
+            const uint64_t X = (uint64_t)(Xc >> D);
+            if (X != 0 && X < (1ull << 53)) {
+              const double x = std::ldexp((double)X, D + eh);
+              if (std::fma(x, yh, x * yl) != x / b) return false;
+            }
+          }
+        }
+        if (D == 54) break;
+      }
+    }
+  }
+  return true;
+}
+
+// Divisor table of the FP64 leapfrog: one slot of {b, RN(1/b), RN((1-b*yh)/b),
+// exact} per distinct divisor b (every spacing value in [2^-40, 2^40], and
+// 1.0), exact = 1.0 when two_op_exact(b), at slot ((lo ^ hi) * mult) >> shift
+// of b's 32-bit halves; mult and the slot count are searched until no two
+// divisors share a slot.  Empty slots hold a bit pattern no divisor has, so
+// they never match.  false: no table (too many distinct values), every
+// division stays the IEEE one.
 static bool build_div_table(const double* const arrs[6], const int lens[6], std::vector<double>& tbl, unsigned* mult,
                             int* shift) {
   std::vector<uint64_t> keys;
@@ -251,7 +294,7 @@ static bool build_div_table(const double* const arrs[6], const int lens[6], std:
         e[0] = b;
         e[1] = yh;
         e[2] = std::fma(-b, yh, 1.0) / b;  // the remainder 1 - b*yh is exact
-        e[3] = 0.0;
+        e[3] = two_op_exact(b, yh, e[2]) ? 1.0 : 0.0;
       }
       *mult = m;
       *shift = sh;

@@ -1,13 +1,15 @@
-"""The FP64 leapfrog's division on isotropic meshes equals IEEE division.
+"""The FP64 leapfrog's divisor-table division equals IEEE division.
 
-On a mesh whose spacings are all one value h, the FP64 path divides by h with
-a double-word reciprocal and one Markstein correction (div_iso in
-phonomena_gb300/csrc/fdtd_step.cu) instead of a general division; the
-reference's results stay bit-identical only if that quotient is the IEEE one
-for every operand.  tests/div_check.c restates the method on the host and
-compares it with x / h bit for bit: random operands over the whole fast
-range, quotients built to lie within about 2^-107 of a rounding midpoint (the
-hard cases), exact multiples, signed zeros and the values that take the
+The FP64 path divides by the mesh's spacings through a table of double-word
+reciprocals (div_tab in phonomena_gb300/csrc/fdtd_step.cu): two operations for
+a divisor the host has proven exact (two_op_exact in csrc/api.cu), one
+Markstein correction more for the others.  The reference's results stay
+bit-identical only if that quotient is the IEEE one for every operand.
+tests/div_check.c restates the method and the exactness check on the host and
+compares the quotient with x / h bit for bit for 256 divisors: random operands
+over the whole fast range, quotients built to lie within |c| * 2^-107 of a
+rounding midpoint for |c| up to 3000 (the hard cases; the check itself looks
+at |c| <= 8), exact multiples, signed zeros and the values that take the
 fallback division.
 """
 from __future__ import annotations
@@ -32,18 +34,23 @@ def div_check(tmp_path_factory):
 
 
 @pytest.mark.parametrize("seed", [1, 2])
-def test_isotropic_division_is_ieee(div_check, seed):
+def test_table_division_is_ieee(div_check, seed):
     out = subprocess.run([str(div_check), "2000000", str(seed)], capture_output=True, text=True)
     cases, bad = (int(v) for v in out.stdout.split()[-2:])
     assert cases > 10_000_000
     assert bad == 0 and out.returncode == 0, out.stdout
 
 
-def test_check_detects_an_uncorrected_quotient(div_check, tmp_path):
-    """Without the remainder correction the near-midpoint cases catch errors,
-    so the check above is not passing vacuously."""
+@pytest.mark.parametrize("weaken", [
+    ("return fma(r, d->yh, q0);", "return q0;"),         # no correction for the inexact divisors
+    ("for (int c = -8; c <= 8; c++) {", "for (int c = 0; c <= 0; c++) {"),  # every divisor taken as exact
+])
+def test_check_detects_a_weakened_method(div_check, tmp_path, weaken):
+    """A weakened method (no remainder correction, or an exactness check that
+    looks at no candidate) gives wrong quotients that the near-midpoint cases
+    catch, so the check above is not passing vacuously."""
     src = (HERE / "div_check.c").read_text()
-    weak = src.replace("return fma(r, d->yh, q0);", "return q0;")
+    weak = src.replace(*weaken)
     assert weak != src
     f = tmp_path / "weak.c"
     f.write_text(weak)
@@ -51,3 +58,54 @@ def test_check_detects_an_uncorrected_quotient(div_check, tmp_path):
     subprocess.run([shutil.which("gcc") or "cc", "-O2", "-ffp-contract=off", "-o", str(exe), str(f), "-lm"], check=True)
     out = subprocess.run([str(exe), "2000000", "1"], capture_output=True, text=True)
     assert int(out.stdout.split()[-1]) > 0
+
+
+# spacing values near 10 um whose two-operation quotient is not exact for
+# every x (found with the check; the FP64 path corrects them), and values of
+# the benchmark meshes, whose quotient is
+INEXACT = [float.fromhex(h) for h in ("0x1.734124667319bp-17", "0x1.67e041ec7f1c3p-17", "0x1.7d89477b95583p-17",
+                                      "0x1.6d2f31fa6e7f3p-17", "0x1.6452afa20d79bp-17", "0x1.8c5e7d6c6587bp-17")]
+EXACT = [float.fromhex(h) for h in ("0x1.4f8b588e368e0p-17", "0x1.4f8b588e368f0p-17", "0x1.4f8b588e368f1p-17",
+                                    "0x1.4f8b588e368f2p-17", "0x1.4f8b588e368f4p-17")] + [1e-5, 1.0, 1.1]
+
+
+def _two_op_failures(b):
+    """x whose RN(x*yh + RN(x*yl)) differs from x / b, over the near-midpoint
+    candidates of the host check, in exact rational arithmetic (Fraction
+    converts to float with round-to-nearest-even)."""
+    import math
+    from fractions import Fraction as Q
+
+    yh = 1.0 / b
+    yl = float(Q(1) - Q(b) * Q(yh)) / b  # the remainder is exact; IEEE division
+    m, e = math.frexp(b)
+    H, eh = int(m * 2 ** 53), e - 53
+    while H % 2 == 0:
+        H //= 2
+        eh += 1
+    inv = pow(H, -1, 2 ** 64)
+    bad = []
+    for D in range(50, 55):
+        for c in range(-8, 9):
+            if c == 0:
+                continue
+            M = (c * inv) % (2 ** D)
+            while M < 2 ** 54:
+                if M >= 2 ** 53 and M % 2 == 1 and (H * M - c) % (2 ** D) == 0:
+                    X = (H * M - c) >> D
+                    if 0 < X < 2 ** 53:
+                        x = math.ldexp(float(X), D + eh)
+                        q = float(Q(x) * Q(yh) + Q(float(Q(x) * Q(yl))))
+                        if q != x / b:
+                            bad.append(x)
+                if D == 54:
+                    break
+                M += 2 ** D
+    return bad
+
+
+def test_exactness_check_restated_in_rational_arithmetic():
+    for b in INEXACT:
+        assert _two_op_failures(b), b.hex()
+    for b in EXACT:
+        assert not _two_op_failures(b), b.hex()

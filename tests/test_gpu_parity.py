@@ -142,6 +142,26 @@ def test_f64_without_divisor_table_vs_oracle(gpu_lib, oracle):
         assert np.array_equal(sim.read_surface(), surf64)
 
 
+def test_f64_corrected_divisors_vs_oracle(gpu_lib, oracle):
+    """Spacings whose two-operation quotient is not exact for every operand
+    (the remainder-corrected path of the divisor table) mixed with exact
+    ones; the result is the oracle's (IEEE division) bit for bit."""
+    from test_division import INEXACT
+
+    d = _crystal_case((48, 40, 24), 60, seed=11)
+    fdx = np.array([INEXACT[q % len(INEXACT)] if q % 3 else d["fdx"][q] for q in range(len(d["fdx"]))])
+    fdy = np.array([INEXACT[(q + 2) % len(INEXACT)] if q % 4 == 1 else d["fdy"][q] for q in range(len(d["fdy"]))])
+    d["fdx"], d["sdx"] = fdx, (fdx[1:] + fdx[:-1]) / 2.0
+    d["fdy"], d["sdy"] = fdy, (fdy[1:] + fdy[:-1]) / 2.0
+    s64, surf64 = oracle.run_f64(_oracle_prob(oracle, d), record_every=10)
+    with device_sim(d, tile_j=8, x_segment=16) as sim:
+        sim.step(60)
+        sim.sync()
+        for key, ref in zip(("ux", "uy", "uz"), s64.u):
+            assert np.array_equal(sim.download(key), ref), key
+        assert np.array_equal(sim.read_surface(), surf64)
+
+
 def test_f64v_matches_reference_arithmetic(gpu_lib):
     """The FP64 velocity form (the fast FP64 error reference) agrees with the
     reference-arithmetic FP64 path to 1e-12 relative L2 over 500 steps."""
