@@ -98,10 +98,25 @@ def listed_segments(planes, length, tail):
     return tuple(length + extra // full + (1 if q < extra % full else 0) for q in range(full)) + tuple(tail)
 
 
+def tapered_count(planes, length):
+    """Segments of x_segment = -length over `planes` planes: length-plane
+    segments while more than 2 * length planes are left, then the rest in
+    four parts (phono_desc.x_segment)."""
+    p = n = 0
+    while planes - p > 2 * length:
+        p += length
+        n += 1
+    rest = planes - p
+    return n + (4 if rest >= 4 else rest)
+
+
 def candidates_for(shape, tile_js=TILE_J):
-    """(tile_j, x_segment) candidates of a mesh: even, tapered and listed segments."""
+    """(tile_j, x_segment) candidates of a mesh: even, tapered and listed
+    segments; tapered and listed ones only where they take at most 64
+    segments (the most a launch describes by table)."""
     planes = int(shape[0]) - 1
-    cands = [(tj, xs) for tj in tile_js for xs in X_SEGMENTS] + [(tj, -xs) for tj in tile_js for xs in X_TAPERED]
+    cands = [(tj, xs) for tj in tile_js for xs in X_SEGMENTS]
+    cands += [(tj, -xs) for tj in tile_js for xs in X_TAPERED if tapered_count(planes, xs) <= 64]
     for tj in tile_js:
         for length in LISTED_L:
             for tail in TAILS:

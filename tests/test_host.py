@@ -180,5 +180,11 @@ def test_listed_segment_candidates_cover_the_planes():
             if isinstance(xs, tuple):
                 assert sum(xs) == shape[0] - 1 and len(xs) <= 64 and min(xs) >= 1
                 assert any(xs[-len(t):] == t for t in autotune.TAILS)
+            elif xs < 0:  # tapered: the launch describes them by table too
+                assert autotune.tapered_count(shape[0] - 1, -xs) <= 64
+    # 1024 planes: -16 would take 66 segments and is left out
+    assert autotune.tapered_count(1024, 16) == 66
+    assert all(xs != -16 for _, xs in autotune.candidates_for((1025, 1025, 257)))
+    assert autotune.tapered_count(256, 28) == 12 and autotune.tapered_count(3, 8) == 3
     assert autotune.listed_segments(256, 30, (16, 12, 8, 6, 4)) == (30,) * 7 + (16, 12, 8, 6, 4)
     assert autotune.listed_segments(40, 36, (16, 12, 8, 6, 4)) is None
