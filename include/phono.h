@@ -39,7 +39,9 @@ extern "C" {
 #define PHONO_ERR_NUMERIC (-5)  /* non-finite value seen in the recorded surface */
 
 /* arithmetic scheme */
-#define PHONO_F64 0  /* reference leapfrog, IEEE op order of the reference */
+#define PHONO_F64 0  /* reference leapfrog in the reference's op order, bit-identical results
+                      * (divisions by the mesh spacings through a table of double-word
+                      * reciprocals, which gives the IEEE quotients) */
 #define PHONO_F32K 1 /* FP32 velocity form, Kahan-compensated displacement */
 #define PHONO_F64V 2 /* the F32K scheme in FP64: fast FP64 reference for error figures */
 
@@ -109,8 +111,8 @@ int phono_create(const phono_desc *desc, phono_handle **out);
  * from update_sin / update_ricker (base_solver.py:294-312). */
 int phono_set_source(phono_handle *h, const double *samples, int n);
 
-/* Advance nsteps time steps; one fused kernel launch per step, replayed from
- * a captured CUDA graph.  Replaces the loop body of BaseSolver.run
+/* Advance nsteps time steps; per step a tile launch and a face launch (one
+ * launch when ny == 3), replayed from captured CUDA graphs of 12 steps.  Replaces the loop body of BaseSolver.run
  * (base_solver.py:245-266): source, update_T, update_T_BC, update_u,
  * update_u_BC, time_step.  Asynchronous on the handle's stream. */
 int phono_step(phono_handle *h, int nsteps);
@@ -182,9 +184,11 @@ int phono_upload_surface(phono_handle *h, int first, int count, const void *host
 /* Element size in bytes of the handle's fields (8 or 4). */
 int phono_elem_size(const phono_handle *h);
 
-/* Kinetic and strain energy of the current state, FP64 accumulation:
- * out[0] = sum rho v^2 / 2 * dV, out[1] = sum T:e / 2 * dV.  No reference
- * counterpart (error metric). */
+/* Kinetic and strain energy of the current state, FP64 accumulation in a
+ * fixed order (the same state gives the same bits): out[0] = sum rho v^2 / 2
+ * over the interior displacement points, out[1] = sum T:e / 2 over the
+ * reference's stress points, unit weights (no cell volume).  Blocks until
+ * done.  No reference counterpart (error metric). */
 int phono_energy(phono_handle *h, double out[2]);
 
 /* Energy of a state held in the caller's own device buffers, computed
@@ -250,8 +254,9 @@ int phono_batch_last_step_ms(phono_batch *b, float *ms);
 void phono_batch_destroy(phono_batch *b);
 
 /* Change the tile shape of a handle (0 keeps a value): tile_j rows per block
- * (4, 8, 16) and x_segment planes per block column.  Results do not depend
- * on the tile shape; the tuner (phonomena_gb300/autotune.py) calls this to
+ * (4, 8, 16) and x_segment planes per block column (-L: tapered, as in
+ * phono_desc; PHONO_ERR_ARG when that takes more than 64 segments).  Results
+ * do not depend on the tile shape; the tuner (phonomena_gb300/autotune.py) calls this to
  * time candidates on one handle.  No reference counterpart. */
 int phono_set_tiling(phono_handle *h, int tile_j, int x_segment);
 
