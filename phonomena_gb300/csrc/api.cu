@@ -200,110 +200,6 @@ static int upload_table(phono_handle* h, const double* table, int nmat, int id00
   return PHONO_OK;
 }
 
-// Whether q0 = RN(x*yh + RN(x*yl)) is the IEEE quotient x/b for every x (no
-// underflow or overflow).  q0 is off x/b by less than 2^-105 relative, so it
-// can round the wrong way only where x/b lies that close to a rounding
-// midpoint mu.  With b = H * 2^e (H odd) and mu = M * 2^f (M odd, 54 bits),
-// x = X * 2^g is that close exactly when H*M = X * 2^D + c with a small
-// integer c (|c| <= 4 follows from the bound; 8 are tried) and D the
-// alignment of X against H*M: M = c * H^-1 mod 2^D.  Every such x (up to a
-// power of two, which scales the quotient exactly) is tried here.  Approach
-// of Brisebarre, Muller and Raina (IEEE Trans. Computers 54(7), 2005).
-static bool two_op_exact(double b, double yh, double yl) {
-  uint64_t hb;
-  std::memcpy(&hb, &b, 8);
-  int eh = (int)((hb >> 52) & 0x7ff) - 1075;
-  uint64_t H = (hb & ((1ull << 52) - 1)) | (1ull << 52);
-  while (!(H & 1)) {
-    H >>= 1;
-    eh++;
-  }
-  uint64_t inv = H;  // H^-1 mod 2^64 by Newton iteration
-  for (int q = 0; q < 6; q++) inv *= 2 - H * inv;
-  for (int D = 50; D <= 54; D++) {
-    const uint64_t mask = (1ull << D) - 1;
-    for (int c = -8; c <= 8; c++) {
-      if (c == 0) continue;
-      for (uint64_t M = ((uint64_t)(int64_t)c * inv) & mask; M < (1ull << 54); M += 1ull << D) {
-        if (M >= (1ull << 53) && (M & 1)) {
-          const unsigned __int128 Xc = (unsigned __int128)H * M - (unsigned __int128)(__int128)c;
-          if ((uint64_t)(Xc & mask) == 0) {
-            const uint64_t X = (uint64_t)(Xc >> D);
-            if (X != 0 && X < (1ull << 53)) {
-              const double x = std::ldexp((double)X, D + eh);
-              if (std::fma(x, yh, x * yl) != x / b) return false;
-            }
-          }
-        }
-        if (D == 54) break;
-      }
-    }
-  }
-  return true;
-}
-
-// Divisor table of the FP64 leapfrog: one slot of {b, RN(1/b), RN((1-b*yh)/b),
-// exact} per distinct divisor b (every spacing value in [2^-40, 2^40], and
-// 1.0), exact = 1.0 when two_op_exact(b), at slot ((lo ^ hi) * mult) >> shift
-// of b's 32-bit halves; mult and the slot count are searched until no two
-// divisors share a slot.  Empty slots hold a bit pattern no divisor has, so
-// they never match.  false: no table (too many distinct values), every
-// division stays the IEEE one.
-static bool build_div_table(const double* const arrs[6], const int lens[6], std::vector<double>& tbl, unsigned* mult,
-                            int* shift) {
-  std::vector<uint64_t> keys;
-  auto add = [&](double b) {
-    if (!(b >= std::ldexp(1.0, -40) && b <= std::ldexp(1.0, 40))) return;
-    uint64_t u;
-    std::memcpy(&u, &b, 8);
-    keys.push_back(u);
-  };
-  add(1.0);
-  for (int a = 0; a < 6; a++)
-    for (int q = 0; q < lens[a]; q++) add(arrs[a][q]);
-  std::sort(keys.begin(), keys.end());
-  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-  auto slot_of = [](uint64_t u, unsigned m, int sh) {
-    return (((unsigned)u ^ (unsigned)(u >> 32)) * m) >> sh;
-  };
-  for (int bits = 4; (1 << bits) <= DIV_TABLE_SLOTS_MAX; bits++) {
-    if ((size_t)(1 << bits) < 2 * keys.size()) continue;
-    const int sh = 32 - bits;
-    for (unsigned k = 0; k < 4096; k++) {
-      const unsigned m = 0x9E3779B1u + 2u * k * 0x632BE5ABu;  // odd multipliers
-      std::vector<char> used((size_t)1 << bits, 0);
-      bool ok = true;
-      for (uint64_t u : keys) {
-        char& c = used[slot_of(u, m, sh)];
-        if (c) {
-          ok = false;
-          break;
-        }
-        c = 1;
-      }
-      if (!ok) continue;
-      const uint64_t empty = ~0ull;
-      double none;
-      std::memcpy(&none, &empty, 8);
-      tbl.assign((size_t)4 * DIV_TABLE_SLOTS_MAX, none);
-      for (uint64_t u : keys) {
-        double b;
-        std::memcpy(&b, &u, 8);
-        const double yh = 1.0 / b;
-        double* e = &tbl[(size_t)4 * slot_of(u, m, sh)];
-        e[0] = b;
-        e[1] = yh;
-        e[2] = std::fma(-b, yh, 1.0) / b;  // the remainder 1 - b*yh is exact
-        e[3] = two_op_exact(b, yh, e[2]) ? 1.0 : 0.0;
-      }
-      *mult = m;
-      *shift = sh;
-      return true;
-    }
-  }
-  return false;
-}
-
 template <class R>
 static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   StepArgs<R> a{};
@@ -684,14 +580,16 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   // spacings
   const double* arrs[6] = {d->fdx, d->fdy, d->fdz, d->sdx, d->sdy, d->sdz};
   int lens[6] = {nx - 1, ny - 1, nz - 1, nx - 2, ny - 2, nz - 2};
-  // FP64 leapfrog: divisor table (div_tab in fdtd_step.cu) over the distinct
+  // FP64 leapfrog: divisor table (div_tab in div_table.cuh) over the distinct
   // spacing values and 1.0, the divisors the step uses
   // (allocated for every FP64 handle, so that phono_footprint is exact)
   if (f64) {
     std::vector<double> tbl;
     double* dt = nullptr;
     TRY(dalloc(h, (void**)&dt, sizeof(double) * 4 * DIV_TABLE_SLOTS_MAX));
-    if (build_div_table(arrs, lens, tbl, &h->dtab.mult, &h->dtab.shift)) {
+    std::vector<double> divisors{1.0};
+    for (int a = 0; a < 6; a++) divisors.insert(divisors.end(), arrs[a], arrs[a] + lens[a]);
+    if (build_div_table(divisors, tbl, &h->dtab.mult, &h->dtab.shift)) {
       TRYC(cudaMemcpy(dt, tbl.data(), tbl.size() * sizeof(double), cudaMemcpyHostToDevice));
       h->dtab.tab = dt;
     }

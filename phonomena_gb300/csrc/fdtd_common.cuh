@@ -24,6 +24,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "div_table.cuh"
+
 namespace phono {
 
 constexpr int TK = 32;      // tile width along z (the contiguous axis): one warp
@@ -66,20 +68,6 @@ struct Spacing {
   R fdx0, fdy0, fdz0, sdx0, sdy0, sdz0;
 };
 
-// Divisor table of the FP64 leapfrog: for each distinct spacing value b of
-// the mesh (and 1.0), entry {b, yh, yl, 0} with yh = RN(1/b) and
-// yl = RN((1 - b*yh)/b), at slot ((lo ^ hi) * mult) >> shift of b's two
-// 32-bit halves (a hash the host picks to be collision-free over the mesh's
-// divisors).  The step divides by b through yh + yl and one remainder
-// correction, which gives the IEEE quotient (div_tab in fdtd_step.cu); a
-// divisor whose slot holds another value takes the IEEE division.
-// tab == nullptr: every division is the IEEE one.
-struct DivTable {
-  const double* tab;  // slots of 4 doubles
-  unsigned mult;
-  int shift;
-};
-constexpr int DIV_TABLE_SLOTS_MAX = 1024;
 
 // Face-point enumeration: for component c and plane p (0 z=N, 1 y=N, 2 y=0,
 // 3 x=N), off[c*4+p] is the first flattened index; off[12] is the total.

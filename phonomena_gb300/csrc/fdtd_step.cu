@@ -41,46 +41,6 @@ namespace phono {
 // ---------------------------------------------------------------------------
 // arithmetic schemes
 // ---------------------------------------------------------------------------
-// x / b rounded to nearest (the IEEE quotient) from the divisor table entry
-// of b: yh = RN(1/b), yl = RN((1 - b*yh)/b),
-//   q0 = RN(x*yh + RN(x*yl))  differs from x/b by less than 2^-105 relative
-//        (yh + yl is 1/b to about 2^-106, and one rounding of that order
-//        follows), so it is within one ulp of x/b; and it is RN(x/b) unless
-//        x/b lies within 2^-105 of a rounding midpoint.  The host enumerates,
-//        for each divisor, every x that comes that close (a handful per
-//        binade, from the odd part of b's significand) and marks b "exact"
-//        when q0 rounds all of them correctly (the approach of Brisebarre,
-//        Muller and Raina, IEEE Trans. Computers 54(7), 2005): then q0 is the
-//        IEEE quotient for every x.
-//   Otherwise r = x - q0*b is exact (one FMA, q0 being within one ulp) and
-//   q = RN(q0 + r*yh) is RN(x/b) by Markstein's theorem (yh within half an
-//        ulp of 1/b, q0 within one ulp of x/b, r exact; P. W. Markstein,
-//        IBM J. Res. Dev. 34(1):111-119, 1990).
-// The argument needs no underflow or overflow on the way, which holds for
-// 2^-800 <= |x| < 2^801 with 2^-40 <= b <= 2^40 (the host enters only such b).
-// Other x (zero, tiny, huge, inf, nan) and divisors without an entry take the
-// IEEE division, except that a zero returns x*yh, the correctly signed zero.
-// Two FP64 operations (four for a divisor that is not exact) against about a
-// dozen of a general division; the lookup and the range tests are integer work.
-__device__ __forceinline__ double div_tab(double x, double b, const DivTable& d) {
-  const unsigned blo = (unsigned)__double2loint(b), bhi = (unsigned)__double2hiint(b);
-  const unsigned slot = ((blo ^ bhi) * d.mult) >> d.shift;
-  const double2* e = reinterpret_cast<const double2*>(d.tab) + 2 * slot;
-  const double2 e0 = __ldg(e);      // b, yh
-  const double2 e1 = __ldg(e + 1);  // yl, exact flag (1.0 or 0.0)
-  const bool hit = (unsigned)__double2loint(e0.x) == blo && (unsigned)__double2hiint(e0.x) == bhi;
-  const unsigned xhi = (unsigned)__double2hiint(x);
-  const unsigned ex = (xhi >> 20) & 0x7ffu;  // biased exponent of x
-  if (!hit || ex - 223u > 1600u) {
-    const bool zero = ((xhi & 0x7fffffffu) | (unsigned)__double2loint(x)) == 0u;
-    return (hit && zero) ? __dmul_rn(x, e0.y) : __ddiv_rn(x, b);
-  }
-  const double q0 = __fma_rn(x, e0.y, __dmul_rn(x, e1.x));
-  if (__double2hiint(e1.y) != 0) return q0;
-  const double r = __fma_rn(-q0, b, x);
-  return __fma_rn(r, e0.y, q0);
-}
-
 struct F64 {
   using R = double;
   static constexpr bool kahan = false;

@@ -1,5 +1,5 @@
-/* Check of the divisor-table division of the FP64 leapfrog (div_tab in
- * phonomena_gb300/csrc/fdtd_step.cu, two_op_exact in csrc/api.cu) against
+/* Check of the divisor-table division of the FP64 leapfrog (div_tab and
+ * two_op_exact in phonomena_gb300/csrc/div_table.cuh) against
  * IEEE division on the host.
  *
  * The method: yh = RN(1/h), yl = RN((1 - h*yh)/h); for 2^-800 <= |x| < 2^801

@@ -1,8 +1,8 @@
 """The FP64 leapfrog's divisor-table division equals IEEE division.
 
 The FP64 path divides by the mesh's spacings through a table of double-word
-reciprocals (div_tab in phonomena_gb300/csrc/fdtd_step.cu): two operations for
-a divisor the host has proven exact (two_op_exact in csrc/api.cu), one
+reciprocals (div_tab in phonomena_gb300/csrc/div_table.cuh): two operations for
+a divisor the host has proven exact (two_op_exact, same file), one
 Markstein correction more for the others.  The reference's results stay
 bit-identical only if that quotient is the IEEE one for every operand.
 tests/div_check.c restates the method and the exactness check on the host and
