@@ -78,3 +78,16 @@ extern "C" int div_check_gpu(const double* x, const double* b, long long n, unsi
   out[3] = fb;
   return rc;
 }
+
+// Host only (no CUDA call): the divisor table build_div_table makes for
+// `values`, for checking the host code on a machine without a GPU.
+// table_out: 4 * slots doubles ({b, yh, yl, exact} per slot, empty slots all
+// ones); returns the slot count, 0 when no table was built.
+extern "C" int div_table_host(const double* values, int n, double* table_out, int table_cap, unsigned* mult,
+                              int* shift) {
+  std::vector<double> tbl;
+  if (!phono::build_div_table(std::vector<double>(values, values + n), tbl, mult, shift)) return 0;
+  if ((int)tbl.size() > table_cap) return -1;
+  std::memcpy(table_out, tbl.data(), tbl.size() * sizeof(double));
+  return (int)(tbl.size() / 4);
+}

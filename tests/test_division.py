@@ -109,3 +109,43 @@ def test_exactness_check_restated_in_rational_arithmetic():
         assert _two_op_failures(b), b.hex()
     for b in EXACT:
         assert not _two_op_failures(b), b.hex()
+
+
+def test_divisor_table_host_code():
+    """build_div_table (the host code phono_create runs, through the test
+    library): every divisor sits at its hash slot with yh = 1/b, yl the
+    rounded remainder term and the exact flag of the rational-arithmetic
+    check; values outside [2^-40, 2^40] get no entry."""
+    import ctypes
+    import math
+    from fractions import Fraction as Q
+
+    import numpy as np
+
+    from phonomena_gb300 import build
+
+    build.build()
+    lib = ctypes.CDLL(str(build.DIV_CHECK_LIB))
+    lib.div_table_host.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int)]
+    rng = np.random.default_rng(3)
+    values = EXACT + INEXACT + [float(v) for v in rng.uniform(0.9e-5, 1.3e-5, 40)] + [math.ldexp(1.0, 41), 0.0]
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    cap = 4 * 4096
+    out = np.empty(cap, dtype=np.float64)
+    mult, shift = ctypes.c_uint(), ctypes.c_int()
+    slots = lib.div_table_host(v.ctypes.data, len(v), out.ctypes.data, cap, ctypes.byref(mult), ctypes.byref(shift))
+    assert slots > 0 and slots & (slots - 1) == 0
+    tab = out[:4 * slots].reshape(slots, 4)
+    bits = tab[:, 0].view(np.uint64)
+    filled = bits != np.uint64(0xFFFFFFFFFFFFFFFF)
+    inside = sorted({b for b in values if 2.0 ** -40 <= b <= 2.0 ** 40})
+    assert filled.sum() == len(inside)
+    for b in inside:
+        u = int(np.float64(b).view(np.uint64))
+        slot = ((((u & 0xFFFFFFFF) ^ (u >> 32)) * mult.value) & 0xFFFFFFFF) >> shift.value
+        e = tab[slot]
+        assert e[0] == b and e[1] == 1.0 / b
+        assert e[2] == float((Q(1) - Q(b) * Q(e[1])) / Q(b))
+        assert (e[3] == 1.0) == (not _two_op_failures(b)), b.hex()
+    assert any(tab[filled, 3] == 0.0) and any(tab[filled, 3] == 1.0)
