@@ -3,7 +3,8 @@
 Run from the repository root where the phonomena sources are available
 (default /root/reference, or PHONO_REFERENCE_ROOT):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                 # every case
+    python tests/golden/make_golden.py fine_json       # named settings-file cases only
 
 Each case runs the reference's unmodified ``solver_default`` through
 ``oracle/ref_harness.py`` (``write_mode='off'``) and stores its inputs (node
@@ -66,9 +67,25 @@ def save(name, out, meta, full=True, check_threading=None):
     print(name, {k: v for k, v in rec.items() if k.startswith("max_")})
 
 
-def main():
+def settings_case(name, rel_path, steps):
+    """A case from one of the reference's own settings files, run as
+    common.loadSettings would set it up (mesh, inclusions, materials, courant)."""
+    g, m, cfg = H.load_settings_case(H.REF_ROOT / rel_path)
+    out = H.run_reference(g, m, steps, wave=cfg["simulation"]["cfg"]["wave"],
+                          wave_args=cfg["simulation"]["cfg"]["wave_args"], record_every=5)
+    save(name, out, dict(steps=steps, record_every=5, wave=cfg["simulation"]["cfg"]["wave"],
+                         surface_mode="reference", bc="absorbing", source_mode="line", settings=rel_path),
+         full=out["ux"].size < 20000)
+
+
+def main(only=None):
     rng = np.random.default_rng(20261203)
     R = H.import_reference()
+    if only:  # only the named cases from the reference's settings files
+        for name, rel_path, steps in SETTINGS_CASES:
+            if name in only:
+                settings_case(name, rel_path, steps)
+        return
 
     # A. the reference's own test setup (base_solver.py:28-70, test_solvers.py:18-23)
     TD = R.base_solver.TestDefaults
@@ -114,15 +131,15 @@ def main():
                                              bc="absorbing", source_mode="line", crystal="config1 seed 0, voids"),
          full=False)
 
-    # I. non-uniform mesh from the reference's own settings file (tests/data/nonuniform.json)
-    g, m, cfg = H.load_settings_case(H.REF_ROOT / "tests" / "data" / "nonuniform.json")
-    out = H.run_reference(g, m, 30, wave=cfg["simulation"]["cfg"]["wave"],
-                          wave_args=cfg["simulation"]["cfg"]["wave_args"], record_every=5)
-    save("nonuniform_json", out, dict(steps=30, record_every=5, wave=cfg["simulation"]["cfg"]["wave"],
-                                      surface_mode="reference", bc="absorbing", source_mode="line",
-                                      settings="tests/data/nonuniform.json"),
-         full=out["ux"].size < 20000)
+    # I-K. the reference's own settings files: a non-uniform mesh, a fine mesh
+    # (0.3-cell spacing) and the application's default, GaAs with Au inclusions
+    for name, rel_path, steps in SETTINGS_CASES:
+        settings_case(name, rel_path, steps)
 
+
+SETTINGS_CASES = (("nonuniform_json", "tests/data/nonuniform.json", 30),
+                  ("fine_json", "tests/data/fine.json", 30),
+                  ("default_json", "data/default.json", 40))
 
 if __name__ == "__main__":
-    main()
+    main(only=set(sys.argv[1:]) or None)
