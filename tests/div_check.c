@@ -32,7 +32,7 @@ static double from_bits(uint64_t u) {
 typedef struct {
   double h, yh, yl;
   int exact;
-} iso_t;
+} entry_t;
 
 /* the host's exactness check of q0 for divisor h (two_op_exact in api.cu) */
 static int two_op_exact(double b, double yh, double yl) {
@@ -68,8 +68,8 @@ static int two_op_exact(double b, double yh, double yl) {
 }
 
 static long long n_exact = 0, n_inexact = 0;
-static iso_t make_iso(double h) {
-  iso_t d;
+static entry_t make_entry(double h) {
+  entry_t d;
   d.h = h;
   d.yh = 1.0 / h;
   d.yl = fma(-h, d.yh, 1.0) / h;
@@ -79,7 +79,7 @@ static iso_t make_iso(double h) {
   return d;
 }
 
-static double div_iso(double x, const iso_t* d) {
+static double div_entry(double x, const entry_t* d) {
   const unsigned e = (unsigned)(bits(x) >> 52) & 0x7ffu;
   if (e - 223u > 1600u) return x == 0.0 ? x * d->yh : x / d->h;
   const double q0 = fma(x, d->yh, x * d->yl);
@@ -105,14 +105,14 @@ static double rnd(unsigned lo, unsigned hi) {
 }
 
 static long long cases = 0, bad = 0;
-static void check(double x, const iso_t* d);
+static void check(double x, const entry_t* d);
 
 /* Quotients within |c| * 2^-107 (relative) of a rounding midpoint, the cases
  * a division method is most likely to round the wrong way.  With h = H * 2^eh
  * (H odd) and a midpoint mu = M * 2^em (M odd, 2^53 <= M < 2^54), pick
  * M = c * H^-1 mod 2^54: then H * M = X * 2^54 + c exactly, so x = X * 2^e
  * is a double and x / h = mu * (1 - c / (H * M)). */
-static void hard_cases(const iso_t* d, int cmax) {
+static void hard_cases(const entry_t* d, int cmax) {
   uint64_t hb = bits(d->h);
   int eh = (int)((hb >> 52) & 0x7ff) - 1075;
   uint64_t H = (hb & ((1ull << 52) - 1)) | (1ull << 52);
@@ -140,8 +140,8 @@ static void hard_cases(const iso_t* d, int cmax) {
     }
   }
 }
-static void check(double x, const iso_t* d) {
-  const double want = x / d->h, got = div_iso(x, d);
+static void check(double x, const entry_t* d) {
+  const double want = x / d->h, got = div_entry(x, d);
   cases++;
   if (isnan(want) ? !isnan(got) : bits(want) != bits(got)) {
     if (bad < 10) printf("mismatch: x=%a h=%a want=%a got=%a\n", x, d->h, want, got);
@@ -163,7 +163,7 @@ int main(int argc, char** argv) {
   while (nh < NH) hs[nh++] = fabs(rnd(1023 - 40, 1023 + 39));
   const long long per = n / nh > 0 ? n / nh : 1;
   for (int t = 0; t < nh; t++) {
-    const iso_t d = make_iso(hs[t]);
+    const entry_t d = make_entry(hs[t]);
     for (long long q = 0; q < per; q++) {
       /* random x over the whole fast range and its edges */
       check(rnd(223, 1823), &d);
