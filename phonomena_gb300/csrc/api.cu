@@ -585,13 +585,13 @@ int phono_create(const phono_desc* d, phono_handle** out) {
   // (allocated for every FP64 handle, so that phono_footprint is exact)
   if (f64) {
     std::vector<double> tbl;
-    double* dt = nullptr;
-    TRY(dalloc(h, (void**)&dt, sizeof(double) * 4 * DIV_TABLE_SLOTS_MAX));
+    double* tab_dev = nullptr;
+    TRY(dalloc(h, (void**)&tab_dev, sizeof(double) * 4 * DIV_TABLE_SLOTS_MAX));
     std::vector<double> divisors{1.0};
     for (int a = 0; a < 6; a++) divisors.insert(divisors.end(), arrs[a], arrs[a] + lens[a]);
     if (build_div_table(divisors, tbl, &h->dtab.mult, &h->dtab.shift)) {
-      TRYC(cudaMemcpy(dt, tbl.data(), tbl.size() * sizeof(double), cudaMemcpyHostToDevice));
-      h->dtab.tab = dt;
+      TRYC(cudaMemcpy(tab_dev, tbl.data(), tbl.size() * sizeof(double), cudaMemcpyHostToDevice));
+      h->dtab.tab = tab_dev;
     }
   }
   // device copies carry one value 1 before and two after the array, so the
