@@ -4,7 +4,7 @@
  *
  * The reference solver is the Python class BaseSolver
  * (phonomena/simulation/base_solver.py:172-571) behind the plugin interface
- * found by common.importSolver / findSolvers (phonomena/common.py:122-145).
+ * found by common.importSolver / findSolvers (phonomena/common.py:88-110).
  * A plugin module (phonomena_gb300/solver_gb300.py) binds these entry points
  * with ctypes; each declaration names the reference code it replaces.
  *
@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHONO_ABI_VERSION 1
+#define PHONO_ABI_VERSION 2
 
 #define PHONO_OK 0
 #define PHONO_ERR_ARG (-1)      /* invalid argument */
@@ -194,24 +194,29 @@ int phono_energy(phono_handle *h, double out[2]);
 /* Energy of a state held in the caller's own device buffers, computed
  * without allocating anything.  No counterpart in the reference.
  *
- * For callers that cannot call cudaMalloc/cudaFree: code that runs while a
- * stream is being captured into a CUDA graph, applications whose device
- * memory is owned by another allocator (a framework's caching pool, a fixed
- * reservation), and latency-bound loops that must not take the implicit
- * device synchronisation of cudaFree.  The per-plane partial sums go to a
- * file-scope __device__ scratch array of PHONO_ENERGY_STATIC_MAX_NX entries
- * (128 KiB, held by every GPU that loads the library until exit); nx above
- * that limit is rejected with PHONO_ERR_ARG.  All calls share that array:
- * calls whose kernels overlap on the GPU race on it and must be serialised
- * by the caller (one stream, or events).  Every call overwrites the partials
- * it reads, so nothing has to be cleared between calls.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
+ * For callers that cannot call cudaMalloc/cudaFree: applications whose
+ * device memory is owned by another allocator (a framework's caching pool, a
+ * fixed reservation made at start-up) and latency-bound loops that must not
+ * take the implicit device synchronisation of cudaFree.  The per-plane
+ * partial sums go to a file-scope __device__ scratch array of
+ * PHONO_ENERGY_STATIC_MAX_NX entries (128 KiB, held by every GPU that loads
+ * the library until the process exits); nx above that limit is rejected
+ * with PHONO_ERR_ARG.  All calls share that array: calls whose kernels
+ * overlap on the GPU race on it and must be serialised by the caller (one
+ * stream, or events).  Every call overwrites the partials it reads, so
+ * nothing has to be cleared between calls.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  The
+ * address is cached for the life of the device's primary context: do not
+ * call this again on a device after cudaDeviceReset.
  *
  * Inputs are dense arrays in the reference shapes, element type given by
  * `precision`, all device pointers; out_dev receives two doubles
  * (kinetic, strain) in device memory, written on `stream` (a cudaStream_t,
- * NULL for the default stream); the call does not synchronise. */
+ * NULL for the default stream); the call does not synchronise.  Material
+ * ids must be below nmat; the kernel checks every id before it reads the
+ * table, and an id at or past nmat makes both outputs NaN (the table is
+ * never read out of bounds). */
 #define PHONO_ENERGY_STATIC_MAX_NX 8192
 
 typedef struct phono_energy_dense {
@@ -219,11 +224,12 @@ typedef struct phono_energy_dense {
   int precision;                 /* PHONO_F64: velocity from (u - u_old)/dt; F32K / F64V: v given */
   const void *ux, *uy, *uz;      /* displacement (float for F32K, double otherwise) */
   const void *vx, *vy, *vz;      /* F32K / F64V: velocity; F64: u at the previous step */
-  const uint8_t *mat;            /* nx*ny*nz node material ids */
-  const double *table;           /* material rows of PHONO_TABLE_COLS doubles */
+  const uint8_t *mat;            /* nx*ny*nz node material ids, each < nmat */
+  const double *table;           /* nmat material rows of PHONO_TABLE_COLS doubles */
   const double *fdx, *fdy, *fdz; /* full spacings (n-1 values) */
   const double *sdx, *sdy, *sdz; /* staggered spacings (n-2 values) */
   double dt;
+  int nmat;                      /* rows of table, 1..256 */
 } phono_energy_dense;
 
 int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *stream);

@@ -1,10 +1,13 @@
-"""Headless runner for the reference phonomena solver (fixture generation only).
+"""Headless runner for the reference phonomena solver.
 
-TEST INFRASTRUCTURE ONLY.  This module imports the reference's own Python
-solver read-only and runs it unmodified through ``BaseSolver.init`` / ``run``
-so that its outputs can be frozen as golden fixtures.  It needs the reference
-sources, which exist only where the fixtures are made; nothing that runs
-against the GPU imports it.
+TEST AND BENCHMARK INFRASTRUCTURE ONLY.  This module imports the reference's
+own Python solver read-only and runs it unmodified through
+``BaseSolver.init`` / ``run``: to freeze its outputs as golden fixtures, to
+run the GB300 plugin inside the reference application in the tests, and to
+time the reference's NumPy solvers in bench.py's reference arm.  The
+reference is found under $PHONO_REFERENCE_ROOT, else in the
+``baseline/_ref`` install made by ``oracle/install_reference.py``.  The
+product package never imports it.
 
 Shims (the reference imports packages that this environment lacks):
   * ``gui.worker.WorkerSignals`` -> a stub with ``status/progress.emit``
@@ -34,7 +37,7 @@ from pathlib import Path
 
 import numpy as np
 
-REF_ROOT = Path(os.environ.get("PHONO_REFERENCE_ROOT", "/root/reference"))
+REF_ROOT = Path(os.environ.get("PHONO_REFERENCE_ROOT") or Path(__file__).resolve().parents[1] / "baseline" / "_ref")
 
 _mods = None
 
@@ -124,7 +127,7 @@ def _install_id_constants(m, ids, names):
 
 
 def load_settings_case(path):
-    """Mirror of common.loadSettings (common.py:147-191) without the solver registry."""
+    """Mirror of common.loadSettings (common.py:112-156) without the solver registry."""
     import json
     R = import_reference()
     cfg = json.load(open(path))

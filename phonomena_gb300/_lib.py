@@ -60,7 +60,7 @@ class PhonoEnergyDense(ctypes.Structure):
         ("mat", ctypes.c_void_p), ("table", ctypes.c_void_p),
         ("fdx", ctypes.c_void_p), ("fdy", ctypes.c_void_p), ("fdz", ctypes.c_void_p),
         ("sdx", ctypes.c_void_p), ("sdy", ctypes.c_void_p), ("sdz", ctypes.c_void_p),
-        ("dt", ctypes.c_double),
+        ("dt", ctypes.c_double), ("nmat", ctypes.c_int),
     ]
 
 

@@ -18,9 +18,6 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libphono_gpu.so"
-# GPU check of the FP64 division (test infrastructure, tests/test_gpu_division.py)
-DIV_CHECK_SRC = ROOT / "tests" / "div_gpu.cu"
-DIV_CHECK_LIB = ROOT / "tests" / "_build" / "libdivcheck.so"
 SOURCES = ["fdtd_step.cu", "energy.cu", "lattice.cu", "api.cu"]
 HEADERS = ["fdtd_common.cuh", "div_table.cuh", "tile_path.cuh", "tile_rows.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -60,10 +57,6 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             if verbose:
                 print(" ".join(cmd), file=sys.stderr)
             procs.append((obj, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
-    if DIV_CHECK_SRC.exists() and (force or _stale(DIV_CHECK_LIB, [DIV_CHECK_SRC, CSRC / "div_table.cuh"])):
-        DIV_CHECK_LIB.parent.mkdir(exist_ok=True)
-        cmd = [cc, *ARCH, *FLAGS, "-I", str(CSRC), "-shared", str(DIV_CHECK_SRC), "-o", str(DIV_CHECK_LIB) + ".tmp"]
-        procs.append((DIV_CHECK_LIB, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     errors = []
     for obj, p in procs:
         out, _ = p.communicate()
@@ -73,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             os.replace(str(obj) + ".tmp", obj)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    if force or any(o != DIV_CHECK_LIB for o, _ in procs) or _stale(LIB, objs):
+    if force or procs or _stale(LIB, objs):
         cmd = [cc, *ARCH, "-shared", "-o", str(LIB) + ".tmp", *map(str, objs)]
         subprocess.run(cmd, check=True, capture_output=not verbose)
         os.replace(str(LIB) + ".tmp", LIB)

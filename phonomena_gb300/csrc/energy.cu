@@ -166,6 +166,8 @@ cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, do
 // array's name to a kernel (it is a host-side stand-in): the device address
 // is looked up once per device with cudaGetSymbolAddress.
 // ---------------------------------------------------------------------------
+#include <atomic>
+
 #include "../../include/phono.h"
 
 namespace phono {
@@ -178,11 +180,20 @@ __global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_d
   const int f32 = a.precision == PHONO_F32K;
   const int vgiven = a.precision != PHONO_F64;
   const double inv_dt = 1.0 / a.dt;
+  const unsigned nmat = (unsigned)a.nmat;
+  bool bad_id = false;  // a material id at or past the table's end: no table read, NaN result
   auto ix = [&](int ii, int jj, int kk) { return ((long long)ii * ny + jj) * nz + kk; };          // ux, mat
   auto iy = [&](int ii, int jj, int kk) { return ((long long)ii * (ny - 1) + jj) * nz + kk; };    // uy
   auto iz = [&](int ii, int jj, int kk) { return ((long long)ii * ny + jj) * (nz - 1) + kk; };    // uz
-  auto rho = [&](int ii, int jj, int kk) { return a.table[a.mat[ix(ii, jj, kk)] * 13 + 12]; };
-  auto C = [&](int ii, int jj, int kk, int e) { return a.table[a.mat[ix(ii, jj, kk)] * 13 + e]; };
+  auto C = [&](int ii, int jj, int kk, int e) {
+    const unsigned id = a.mat[ix(ii, jj, kk)];
+    if (id >= nmat) {
+      bad_id = true;
+      return 0.0;
+    }
+    return a.table[id * 13 + e];
+  };
+  auto rho = [&](int ii, int jj, int kk) { return C(ii, jj, kk, 12); };
   auto vel = [&](const void* u, const void* v, long long off) {
     double x = ld(v, f32, off);
     return vgiven ? x : (ld(u, 0, off) - x) * inv_dt;
@@ -227,6 +238,7 @@ __global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_d
       es += 0.5 * C(i + 1, j + 1, k, 11) * gam * gam;
     }
   }
+  const bool any_bad = __syncthreads_or(bad_id);
   __shared__ double sk[EN_THREADS], ss[EN_THREADS];
   sk[threadIdx.x] = ek;
   ss[threadIdx.x] = es;
@@ -238,7 +250,9 @@ __global__ void __launch_bounds__(EN_THREADS) energy_plane_kernel(phono_energy_d
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) partial[i] = make_double2(sk[0], ss[0]);
+  if (threadIdx.x == 0) partial[i] = any_bad ? make_double2(__longlong_as_double(0x7ff8000000000000LL),
+                                                            __longlong_as_double(0x7ff8000000000000LL))
+                                             : make_double2(sk[0], ss[0]);
 }
 
 }  // namespace phono
@@ -248,9 +262,14 @@ void set_last_error(const char* msg);  // api.cu: message behind phono_last_erro
 }
 
 namespace {
-// device address of g_energy_scratch, looked up once per device
+// Device address of g_energy_scratch, looked up on the first call made with
+// that device current.  Two host threads making their first call on one
+// device at the same time both look it up and store the same value; the
+// atomics make that well defined.  The address belongs to the device's
+// primary context: after cudaDeviceReset the cache is stale, so a process
+// that resets a device must not call phono_energy_static on it again.
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {};
+std::atomic<void*> g_scratch_addr[kMaxDevices];
 }  // namespace
 
 extern "C" int phono_energy_static(const phono_energy_dense* in, double* out_dev, void* stream) {
@@ -270,16 +289,17 @@ extern "C" int phono_energy_static(const phono_energy_dense* in, double* out_dev
       !in->fdy || !in->fdz || !in->sdx || !in->sdy || !in->sdz)
     return fail(PHONO_ERR_ARG, "NULL device pointer in the input");
   if (!(in->dt > 0.0)) return fail(PHONO_ERR_ARG, "dt must be > 0");
+  if (in->nmat < 1 || in->nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(PHONO_ERR_CUDA, "cudaGetDevice failed");
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_energy_scratch);
-    if (e != cudaSuccess || !p) return fail(PHONO_ERR_CUDA, "cudaGetSymbolAddress of the energy scratch failed");
-    g_scratch_addr[dev] = p;
+  void* addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_energy_scratch);
+    if (e != cudaSuccess || !addr) return fail(PHONO_ERR_CUDA, "cudaGetSymbolAddress of the energy scratch failed");
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  double2* partial = static_cast<double2*>(g_scratch_addr[dev]);
+  double2* partial = static_cast<double2*>(addr);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   energy_plane_kernel<<<in->nx, EN_THREADS, 0, st>>>(*in, partial);
   energy_final_kernel<<<1, EN_THREADS, 0, st>>>(partial, in->nx, out_dev);

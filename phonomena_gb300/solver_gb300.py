@@ -1,7 +1,7 @@
 """GB300 solver plugin for phonomena (drop-in ``Solver`` class).
 
 Copy or symlink this module into ``phonomena/simulation/solvers/`` (or import
-it from there): ``common.findSolvers`` (phonomena/common.py:128-145) then
+it from there): ``common.findSolvers`` (phonomena/common.py:93-110) then
 finds a solver named ``gb300`` and ``common.loadSettings`` selects it with
 ``"solver": "gb300"``.  Inside phonomena the class subclasses the
 reference's ``simulation.base_solver.BaseSolver``; standalone it subclasses

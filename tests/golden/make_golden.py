@@ -1,7 +1,8 @@
 """Generate the golden fixtures of tests/golden/ by running the reference solver.
 
 Run from the repository root where the phonomena sources are available
-(default /root/reference, or PHONO_REFERENCE_ROOT):
+(the baseline/_ref install made by oracle/install_reference.py, or
+$PHONO_REFERENCE_ROOT):
 
     python tests/golden/make_golden.py                 # every case
     python tests/golden/make_golden.py fine_json       # named settings-file cases only

@@ -122,10 +122,9 @@ def test_divisor_table_host_code():
 
     import numpy as np
 
-    from phonomena_gb300 import build
+    from conftest import build_divcheck
 
-    build.build()
-    lib = ctypes.CDLL(str(build.DIV_CHECK_LIB))
+    lib = ctypes.CDLL(str(build_divcheck()))
     lib.div_table_host.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                    ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int)]
     rng = np.random.default_rng(3)

@@ -19,6 +19,7 @@ import math
 import numpy as np
 import pytest
 
+from conftest import build_divcheck
 from test_division import EXACT, INEXACT
 
 pytestmark = pytest.mark.gpu
@@ -55,10 +56,7 @@ def _near_midpoint_x(b, cmax=64, exps=(-500, -250, 0, 250, 500)):
 
 @pytest.fixture(scope="module")
 def divcheck():
-    from phonomena_gb300 import build
-
-    build.build()
-    lib = ctypes.CDLL(str(build.DIV_CHECK_LIB))
+    lib = ctypes.CDLL(str(build_divcheck()))
     lib.div_check_gpu.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
                                   ctypes.POINTER(ctypes.c_ulonglong)]
     lib.div_check_gpu.restype = ctypes.c_int

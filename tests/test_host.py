@@ -92,11 +92,11 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, name), f"{name} declared in include/phono.h but not exported"
     assert set(_lib.EXPORTS) >= set(declared)
     L.phono_abi_version.restype = ctypes.c_int
-    assert L.phono_abi_version() == 1
+    assert L.phono_abi_version() == 2
 
 
 def test_plugin_is_discoverable_like_common_findSolvers(tmp_path, monkeypatch):
-    """Mimic phonomena/common.py:122-145: import simulation.solvers.<module>, read Solver().name."""
+    """Mimic phonomena/common.py:88-110: import simulation.solvers.<module>, read Solver().name."""
     pkg = tmp_path / "simulation" / "solvers"
     pkg.mkdir(parents=True)
     (tmp_path / "simulation" / "__init__.py").write_text("")
@@ -111,7 +111,7 @@ def test_plugin_is_discoverable_like_common_findSolvers(tmp_path, monkeypatch):
     assert s.name == "gb300"
     assert {"wave", "wave_args", "write_mode", "precision", "record_every"} <= set(s.cfg)
     import json
-    json.dumps(s.cfg)  # cfg stays JSON-serialisable (common.py:213-216)
+    json.dumps(s.cfg)  # cfg stays JSON-serialisable (common.py:178, json.dump of solver.cfg in saveSettings)
 
 
 def test_output_npz_schema(tmp_path):

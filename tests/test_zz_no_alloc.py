@@ -1,9 +1,9 @@
 """The allocation-free energy entry point, phono_energy_static.
 
-Some callers cannot call cudaMalloc: code that runs while a stream is being
-captured into a CUDA graph, applications whose device memory belongs to
-another allocator, and latency-bound loops that must not take cudaFree's
-implicit device synchronisation.  phono_energy_static serves them: it reads
+Some callers cannot call cudaMalloc: applications whose device memory
+belongs to another allocator (a framework's caching pool, a reservation made
+at start-up) and latency-bound loops that must not take cudaFree's implicit
+device synchronisation.  phono_energy_static serves them: it reads
 the caller's own device arrays and keeps its partial sums in a static
 __device__ array instead of allocating.  These tests call it through the C
 ABI on dense copies of a solver state and check it against phono_energy (the
@@ -42,7 +42,7 @@ def _dense_inputs(sim, g, m, precision):
 
     from phonomena_gb300 import _lib
 
-    vel = ("vx", "vy", "vz") if precision == "f32k" else ("ux_old", "uy_old", "uz_old")
+    vel = ("ux_old", "uy_old", "uz_old") if precision == "f64" else ("vx", "vy", "vz")
     keep = {k: torch.from_numpy(np.ascontiguousarray(sim.download(k))).cuda() for k in ("ux", "uy", "uz") + vel}
     keep["mat"] = torch.from_numpy(np.ascontiguousarray(m.ids)).cuda()
     keep["table"] = torch.from_numpy(np.ascontiguousarray(m.table, dtype=np.float64)).cuda()
@@ -53,11 +53,11 @@ def _dense_inputs(sim, g, m, precision):
                               *(keep[k].data_ptr() for k in ("ux", "uy", "uz") + vel),
                               keep["mat"].data_ptr(), keep["table"].data_ptr(),
                               *(keep[k].data_ptr() for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")),
-                              float(m.dt))
+                              float(m.dt), int(m.table.shape[0]))
     return d, keep
 
 
-@pytest.mark.parametrize("precision", ["f64", "f32k"])
+@pytest.mark.parametrize("precision", ["f64", "f32k", "f64v"])
 def test_energy_static_matches_allocating_entry_point(gpu_lib, precision):
     import torch
 
@@ -89,3 +89,23 @@ def test_energy_static_rejects_grids_beyond_the_scratch(gpu_lib):
     rc = gpu_lib.phono_energy_static(ctypes.byref(d), 16, None)
     assert rc == -1
     assert b"PHONO_ENERGY_STATIC_MAX_NX" in gpu_lib.phono_last_error()
+
+
+def test_energy_static_flags_material_ids_past_the_table(gpu_lib):
+    """A material id at or past nmat is not used to index the table: both
+    outputs come back NaN (a table of one row, ids up to 2)."""
+    import torch
+
+    from phonomena_gb300._lib import check
+
+    sim, g, m = _state("f64")
+    d, keep = _dense_inputs(sim, g, m, "f64")
+    assert int(m.ids.max()) >= 1
+    d.nmat = 1
+    out = torch.zeros((2,), dtype=torch.float64, device="cuda")
+    check(gpu_lib.phono_energy_static(ctypes.byref(d), out.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert np.isnan(out.cpu().numpy()).all()
+    d.nmat = 0
+    assert gpu_lib.phono_energy_static(ctypes.byref(d), out.data_ptr(), None) == -1
+    sim.close()
