@@ -59,6 +59,16 @@ def parse():
     p.add_argument("--x-segment", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-precision", action="store_true",
+                   help="crystal: leave out the 1024x1024x256 FP32K-vs-FP64 error study (precision_config3)")
+    p.add_argument("--precision-cells", default="1024,1024,256")
+    p.add_argument("--precision-steps", type=int, default=4000)
+    p.add_argument("--no-serve", action="store_true", help="crystal: leave out the served-latency streams (serve)")
+    p.add_argument("--serve-requests", type=int, default=500, help="crystal: FP32K requests per served stream")
+    p.add_argument("--serve-loads", default="0.7,0.9", help="crystal: FP32K offered loads (fractions of 45 Gcell/s)")
+    p.add_argument("--serve-requests-f64", type=int, default=200, help="crystal: plain FP64 served requests")
+    p.add_argument("--no-reference-numpy", action="store_true",
+                   help="reference: leave out the timing of phonomena's own NumPy solvers")
     return p.parse_args()
 
 
@@ -170,6 +180,49 @@ def cpu_oracle_rate(cells, seconds, seed=0):
     return spec.n_nodes * (done - 1) / t / 1e9, threads, done - 1, t
 
 
+def reference_numpy(cases=(("config1", 500), ("config2", 20)), solvers=("default", "threading")):
+    """phonomena's own NumPy solvers (the reference itself, from the
+    baseline/_ref install) timed on this host: solver_default (NumPy
+    elementwise, one core) and solver_threading (cfg num_threads = 6,
+    solver_threading.py:10), FP64, writer off, through oracle/ref_harness.py.
+    config1: the 40x40x20-cell void crystal for its full 500 steps; config2:
+    the 256x256x128-cell crystal for 20 of its 2000 steps (a bounded sample;
+    its per-node 6x6 C array alone is 2.45 GB).  Time = BaseSolver.run only
+    (init, which fills C and P, is not timed)."""
+    from oracle import ref_harness as H
+    from phonomena_gb300 import crystal
+
+    if not H.available():
+        return {"unavailable": f"reference application not installed under {H.REF_ROOT}"}
+    H.import_reference()
+    mats = [dict(crystal.HOST), dict(crystal.VOID), dict(crystal.TUNGSTEN)]
+    out = {"cpu_count": os.cpu_count(),
+           "affinity": len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else None,
+           "arithmetic": "FP64, the reference's own NumPy code (no FMA, reference op order)"}
+    for name, steps in cases:
+        spec = crystal.config1(seed=0) if name == "config1" else crystal.config2(seed=0)
+        ids = crystal.material_ids(spec)
+        g, m = H.make_uniform_case(spec.cells, 10e-6, mats, ids, c_max=0.5 / 10e-6, primary=0, secondary=2)
+        for solver in solvers:
+            R = H.import_reference()
+            mod = {"default": R.solver_default, "threading": R.solver_threading}[solver]
+            sv = mod.Solver()
+            sv.cfg.update(write_mode="off", wave="sin", wave_args={"f": spec.freq})
+            sv.init(g, m, steps)
+            H._install_id_constants(sv.m, ids, [mm["name"] for mm in mats])
+            sv.m.update()
+            t0 = time.perf_counter()
+            sv.run()
+            el = time.perf_counter() - t0
+            out[f"{name}_{solver}"] = {
+                "value": round(spec.n_nodes * steps / el / 1e9, 6), "unit": "Gcell-updates/s",
+                "seconds": round(el, 3), "time_steps": steps, "nodes": spec.n_nodes,
+                "threads": 1 if solver == "default" else int(sv.cfg.get("num_threads", 6)),
+                "sample": "full run" if name == "config1" else f"{steps} of the 2000 time steps"}
+            del sv
+    return out
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -203,6 +256,8 @@ def reference_arm(args, rank, world):
                                    "arithmetic (oracle/cpu_ref.c, OpenMP)"},
         "e2e": {"value": round(val, 6), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_reference_numpy:
+        line["reference_numpy"] = reference_numpy()
     print(json.dumps(line), flush=True)
 
 
@@ -384,41 +439,55 @@ def bench_batch(args, rank, world, local, torch, dist):
         print(json.dumps(line), flush=True)
 
 
-def bench_serve(args, rank, world, local, torch, dist):
-    """Poisson stream of crystal-simulation requests (config-4 size mix plus
-    5% 512x512x128-cell jobs, 500-3000 steps each, surface uz every 10
-    steps) served by continuous batching under a device-memory budget; FP32K
-    and plain FP64 streams, each at about 70% of its own throughput."""
+SERVE_GCELL = {"f32k": 45.0, "f64": 4.0}  # batched throughputs the offered loads refer to
+
+
+def serve_stream(precision, n, rate, seed, budget_gb):
+    """One Poisson stream of crystal-simulation requests (config-4 size mix
+    plus 5% 512x512x128-cell jobs, 500-3000 steps each, surface uz every 10
+    steps) served by continuous batching under a device-memory budget:
+    latency percentiles, served throughput and admission statistics."""
     from phonomena_gb300 import serve
 
-    budget = args.budget_gb * 1e9
-    gcell32, gcell64 = 45.0, 4.0  # batched throughputs used to set the default rates
-    rate32 = args.rate or serve.rate_for_load(gcell32, 0.7)
-    rate64 = rate32 * gcell64 / gcell32
+    reqs = serve.poisson_stream(n, rate, seed=seed)
+    be = serve.GpuBackend(precision=precision, capacity=256, max_steps=3000)
+    srv = serve.Server(be, budget_bytes=budget_gb * 1e9, capacity=256, chunk=60)
+    streamed = []
+    srv.on_result = lambda r: streamed.append(r.surface.nbytes)
+    t0 = time.perf_counter()
+    res = srv.run(reqs, realtime=True)
+    wall = time.perf_counter() - t0
+    srv.close()
+    be.close()
+    out = serve.summarize(res)
+    out.update({"rate_per_s": round(rate, 4), "offered_gcell_per_s": round(rate * serve.mean_work() / 1e9, 3),
+                "wall_s": round(wall, 2), "peak_resident_gb": round(srv.stats.peak_bytes / 1e9, 2),
+                "peak_active": srv.stats.peak_active, "chunks": srv.stats.chunks,
+                "rejected": len(srv.stats.rejected), "streamed_surface_bytes": int(sum(streamed))})
+    return out
 
-    def run(precision, n, rate, seed):
-        reqs = serve.poisson_stream(n, rate, seed=seed)
-        be = serve.GpuBackend(precision=precision, capacity=256, max_steps=3000)
-        srv = serve.Server(be, budget_bytes=budget, capacity=256, chunk=60)
-        streamed = []
-        srv.on_result = lambda r: streamed.append(r.surface.nbytes)
-        t0 = time.perf_counter()
-        res = srv.run(reqs, realtime=True)
-        wall = time.perf_counter() - t0
-        srv.close()
-        be.close()
-        out = serve.summarize(res)
-        out.update({"rate_per_s": round(rate, 4), "offered_gcell_per_s": round(rate * serve.mean_work() / 1e9, 3),
-                    "wall_s": round(wall, 2), "peak_resident_gb": round(srv.stats.peak_bytes / 1e9, 2),
-                    "peak_active": srv.stats.peak_active, "chunks": srv.stats.chunks,
-                    "rejected": len(srv.stats.rejected), "streamed_surface_bytes": int(sum(streamed))})
-        return out
 
+def serve_summary(r, load):
+    """The served-stream figures of the benchmark line."""
+    return {"load": load, "rate": r["rate_per_s"], "requests": r["requests"], "p50": round(r["p50_s"], 4),
+            "p95": round(r["p95_s"], 4), "p99": round(r["p99_s"], 4),
+            "gcell_per_s": round(r["gcell_updates_per_s"], 4), "offered_gcell_per_s": r["offered_gcell_per_s"],
+            "failed": r["failed"], "rejected": r["rejected"], "peak_active": r["peak_active"],
+            "peak_resident_gb": r["peak_resident_gb"], "wall_s": r["wall_s"]}
+
+
+def bench_serve(args, rank, world, local, torch, dist):
+    """FP32K and plain FP64 request streams, each at about 70% of its own
+    batched throughput (serve_stream)."""
+    from phonomena_gb300 import serve
+
+    rate32 = args.rate or serve.rate_for_load(SERVE_GCELL["f32k"], 0.7)
+    rate64 = rate32 * SERVE_GCELL["f64"] / SERVE_GCELL["f32k"]
     bus = getattr(torch.cuda.get_device_properties(local), "pci_bus_id", "")
     with ClockSampler(bus) as clk:
-        r32 = run("f32k", args.requests, rate32, seed=rank)
+        r32 = serve_stream("f32k", args.requests, rate32, rank, args.budget_gb)
     clocks = clk.summary()
-    r64 = run("f64", args.requests_f64, rate64, seed=rank + 1000)
+    r64 = serve_stream("f64", args.requests_f64, rate64, rank + 1000, args.budget_gb)
     if rank == 0:
         line = {
             "metric": "served Gcell-updates/s", "value": round(r32["gcell_updates_per_s"], 4),
@@ -426,8 +495,8 @@ def bench_serve(args, rank, world, local, torch, dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded request stream)",
             "config": {"workload": f"Poisson stream of {args.requests} requests at {rate32:.3f}/s (70% of "
-                                   f"{gcell32} Gcell/s offered), sizes {{64..192}}^2 x {{32..96}} cells plus 5% "
-                                   "512x512x128, 500-3000 steps, uz surface every 10 steps, "
+                                   f"{SERVE_GCELL['f32k']} Gcell/s offered), sizes {{64..192}}^2 x {{32..96}} cells "
+                                   "plus 5% 512x512x128, 500-3000 steps, uz surface every 10 steps, "
                                    f"{args.budget_gb:.0f} GB device budget, continuous batching",
                        "parallelism": f"replicas x{world}"},
             "latency_s": {"p50": round(r32["p50_s"], 4), "p95": round(r32["p95_s"], 4), "p99": round(r32["p99_s"], 4)},
@@ -436,19 +505,38 @@ def bench_serve(args, rank, world, local, torch, dist):
         print(json.dumps(line), flush=True)
 
 
-def bench_precision(args, rank, world, local, torch, dist):
-    """1024x1024x256-cell seeded crystal (config-2 recipe), 4000 steps: FP32
+def serve_study(args, rank):
+    """The serve object of the default line: FP32K streams at the offered
+    loads of --serve-loads, a plain FP64 stream at 70% of its throughput."""
+    from phonomena_gb300 import serve
+
+    loads = [float(v) for v in args.serve_loads.split(",") if v]
+    out = {"workload": "Poisson request streams: sizes {64..192}^2 x {32..96} cells plus 5% 512x512x128, "
+                       "500-3000 steps, uz surface every 10 steps, continuous batching, "
+                       f"{args.budget_gb:.0f} GB device budget; load = offered work / the scheme's batched "
+                       f"throughput ({SERVE_GCELL['f32k']} Gcell/s FP32K, {SERVE_GCELL['f64']} FP64)",
+           "f32k": [], "fp64": []}
+    for q, load in enumerate(loads):
+        rate = serve.rate_for_load(SERVE_GCELL["f32k"], load)
+        out["f32k"].append(serve_summary(serve_stream("f32k", args.serve_requests, rate, rank + 10 * q,
+                                                      args.budget_gb), load))
+    rate64 = serve.rate_for_load(SERVE_GCELL["f64"], 0.7)
+    out["fp64"].append(serve_summary(serve_stream("f64", args.serve_requests_f64, rate64, rank + 1000,
+                                                  args.budget_gb), 0.7))
+    return out
+
+
+def precision_study(cells, S, seed, torch):
+    """Seeded crystal of the config-2 recipe on a cells grid, S steps: FP32
     fields with Kahan-compensated u against the plain FP64 path (the
     reference arithmetic) on the same inputs; relative L2 error of surface
-    uz and of the total energy after 1000, 2000 and 4000 steps, and the
-    throughput of both runs."""
+    uz and relative error of the total energy after S/4, S/2 and S steps, and
+    the device throughput of both runs."""
     from phonomena_gb300 import autotune
     from phonomena_gb300.device import DeviceSimulation
 
-    cells = (1024, 1024, 256) if args.cells == "256,256,128" else tuple(int(c) for c in args.cells.split(","))
-    S = args.fdtd_steps or 4000
     marks = [m for m in (S // 4, S // 2, S) if m > 0]
-    spec, g, m, src = workload(cells, rank, S)
+    spec, g, m, src = workload(cells, seed, S)
     sp = g.spacing()
     every = S // 4
 
@@ -486,18 +574,31 @@ def bench_precision(args, rank, world, local, torch, dist):
     nodes = spec.n_nodes
     v32 = nodes * S / (r32["ms"] / 1e3) / 1e9
     v64 = nodes * S / (r64["ms"] / 1e3) / 1e9
+    worst = max(max(v["rel_l2_surface_uz"], v["rel_energy"]) for v in per.values())
+    return {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({nodes} nodes), {S} time steps, "
+                        "FP32K vs plain FP64 on the same inputs (config-2 recipe, seed 0)",
+            "nodes": nodes, "fdtd_steps": S, "errors_at_step": per, "max_error": worst, "tolerance": 1e-5,
+            "within_tolerance": bool(worst <= 1e-5),
+            "f32k": {"value": round(v32, 4), "unit": "Gcell-updates/s", "ms": round(r32["ms"], 1),
+                     "tile": r32["tile"]},
+            "fp64": {"value": round(v64, 4), "unit": "Gcell-updates/s", "ms": round(r64["ms"], 1),
+                     "tile": r64["tile"]},
+            "speedup_f32k_over_f64": round(v32 / v64, 3)}
+
+
+def bench_precision(args, rank, world, local, torch, dist):
+    """The precision study (precision_study) as its own benchmark line."""
+    cells = (1024, 1024, 256) if args.cells == "256,256,128" else tuple(int(c) for c in args.cells.split(","))
+    S = args.fdtd_steps or 4000
+    r = precision_study(cells, S, rank, torch)
     if rank == 0:
-        line = {"metric": "rel L2 error FP32K vs FP64", "value": max(v["rel_l2_surface_uz"] for v in per.values()),
+        line = {"metric": "rel L2 error FP32K vs FP64",
+                "value": max(v["rel_l2_surface_uz"] for v in r["errors_at_step"].values()),
                 "unit": "relative L2", "higher_is_better": False, "n_gpus": world, "steps": 1, "warmup": 0,
                 "dtype": "f32", "data": "synthetic (seeded crystal)",
-                "config": {"workload": f"crystal {cells[0]}x{cells[1]}x{cells[2]} cells ({nodes} nodes), {S} time "
-                                       "steps, FP32K vs plain FP64 on the same inputs", "nodes": nodes},
-                "errors_at_step": per,
-                "f32k": {"value": round(v32, 4), "unit": "Gcell-updates/s", "ms": round(r32["ms"], 1),
-                         "tile": r32["tile"]},
-                "fp64": {"value": round(v64, 4), "unit": "Gcell-updates/s", "ms": round(r64["ms"], 1),
-                         "tile": r64["tile"]},
-                "speedup_f32k_over_f64": round(v32 / v64, 3)}
+                "config": {"workload": r["workload"], "nodes": r["nodes"]},
+                "errors_at_step": r["errors_at_step"], "f32k": r["f32k"], "fp64": r["fp64"],
+                "speedup_f32k_over_f64": r["speedup_f32k_over_f64"]}
         print(json.dumps(line), flush=True)
 
 
@@ -584,9 +685,17 @@ def main():
     surf32 = sim.read_surface().astype(np.float64)
     u32 = [sim.download(k).astype(np.float64) for k in ("ux", "uy", "uz")]
     e32 = sim.energy()
-    launch_ms = ms / (args.steps * S)
+    step_ms = ms / (args.steps * S)
+    # the stencil kernel alone: CUDA events around each tile launch (and
+    # apart, each face launch) of KT steps, launched back to back
+    KT = min(240, S)
+    sim.reset()
+    tile_ms, face_ms = sim.time_kernels(KT)
+    sim.sync()
+    launch_ms = tile_ms / KT
     hbm_peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_NODE * nodes / (launch_ms / 1e3) / 1e9
+    step_achieved = BYTES_PER_NODE * nodes / (step_ms / 1e3) / 1e9
     tpn = traffic_per_node("fdtd_step_kernel_f32k")
 
     # ---- FP64 on the same crystal, one full run each: the reference
@@ -657,6 +766,13 @@ def main():
     e2e = world * nodes * S * args.steps / wall / 1e9
     sim.close()
 
+    # ---- the untimed studies of the line: config-3 error table, served latency ----
+    prec3 = None
+    if not args.no_precision:
+        pc = tuple(int(c) for c in args.precision_cells.split(","))
+        prec3 = precision_study(pc, args.precision_steps, rank, torch)
+    served = None if args.no_serve else serve_study(args, rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, threads, nst, secs = cpu_oracle_rate(cells, args.cpu_seconds)
@@ -689,14 +805,21 @@ def main():
                          "traffic": (round(tpn * nodes) if tpn else None),
                          "algorithmic_bytes_per_launch": BYTES_PER_NODE * nodes,
                          "avg_launch_ms": round(launch_ms, 5),
-                         "launch_timing": "one time step = tile pass + face pass (+1/12 counter update); "
-                                          "the whole step is charged to the stencil kernel"},
+                         "launch_timing": f"fdtd_step_kernel<F32K> alone: CUDA events on the solver's stream around "
+                                          f"each tile launch of {KT} back-to-back steps (phono_time_kernels)",
+                         "face_launch_ms": round(face_ms / KT, 5),
+                         "whole_step": {"ms": round(step_ms, 5), "achieved": round(step_achieved, 1),
+                                        "frac": round(step_achieved / hbm_peak, 4),
+                                        "note": "graph-replayed step of the timed region: tile + face launch "
+                                                "(+1/12 counter update), all charged to the stencil"}},
             "tile": list(shapes["f32k"]),
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": graph_launches(S, separate_faces) * args.steps,
             "clocks": clocks,
+            "precision_config3": prec3,
+            "serve": served,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -37,6 +37,7 @@ extern "C" {
 #define PHONO_ERR_NOMEM (-3)    /* device or host allocation failed / over budget */
 #define PHONO_ERR_STATE (-4)    /* call not valid in the current state */
 #define PHONO_ERR_NUMERIC (-5)  /* non-finite value seen in the recorded surface */
+#define PHONO_ERR_TIMEOUT (-6)  /* a bounded device wait ran out; the state of that step is invalid */
 
 /* arithmetic scheme */
 #define PHONO_F64 0  /* reference leapfrog in the reference's op order, bit-identical results
@@ -117,6 +118,14 @@ int phono_set_source(phono_handle *h, const double *samples, int n);
  * update_u_BC, time_step.  Asynchronous on the handle's stream. */
 int phono_step(phono_handle *h, int nsteps);
 
+/* Advance nsteps time steps like phono_step, but without the graph and with
+ * a CUDA event before and after each launch, so that the two kernels of a
+ * step are timed apart: *tile_ms = the summed device time of the tile
+ * launches (the fused launch when ny == 3), *face_ms = that of the face
+ * launches.  Blocks until done.  Results are those of phono_step.  No
+ * reference counterpart (measurement). */
+int phono_time_kernels(phono_handle *h, int nsteps, float *tile_ms, float *face_ms);
+
 /* Global steps completed so far (host-side count of enqueued steps). */
 int phono_steps_done(const phono_handle *h);
 
@@ -150,13 +159,61 @@ typedef struct phono_lattice {
 
 int phono_set_lattice(phono_handle *h, const phono_lattice *lat, const double *table, int nmat);
 
+/* Material ids of the reference's inclusion model, built on the device.
+ * Replaces Material.setConstants (phonomena/simulation/material.py:55-63)
+ * with the inclusion search of Grid.inclusionIndices
+ * (phonomena/simulation/grid.py:158-175), on any mesh the reference builds
+ * (non-uniform x and y included), without the per-node 6x6 C and P arrays.
+ *
+ * An inclusion is a vertical cylinder as Grid.targets holds it: centre
+ * (tx, ty), radius tr and depth tz in mesh units, float32 (the reference's
+ * trgt_dtype).  Node (i, j, k) lies in inclusion t when
+ *   sqrt((x[i] - tx)^2 + (y[j] - ty)^2) < tr     (FP64, as NumPy computes it)
+ * and k is in the inclusion's z selection.  The z selection reproduces the
+ * reference exactly, including how grid.py:174 rebinds `z`: the first
+ * inclusion keeps the nodes with z[k] <= tz; each later inclusion keeps the
+ * node indices p < (the previous selection's length) with p <= tz.  Where
+ * inclusions overlap, the later one in the list wins (the reference
+ * overwrites in list order).  Every other node gets `host`.
+ *
+ * x, y, z are the node coordinates (Grid.x, Grid.y, Grid.z: nx, ny, nz
+ * values, strictly ascending, host memory).  The table as in
+ * phono_set_materials; the absorbing faces take their wave speeds from the
+ * material that ends up at node (0, 0, 0). */
+typedef struct phono_inclusions {
+  const double *x, *y, *z;        /* node coordinates in mesh units */
+  int n;                          /* inclusions (rows of Grid.targets), >= 0 */
+  const float *tx, *ty, *tz, *tr; /* Grid.targets fields x, y, z, r */
+  const uint8_t *id;              /* material id of each inclusion; NULL: all `inside` */
+  int inside;                     /* id of every inclusion when id is NULL (the secondary material) */
+  int host;                       /* id outside the inclusions (the primary material) */
+} phono_inclusions;
+
+int phono_set_inclusions(phono_handle *h, const phono_inclusions *inc, const double *table, int nmat);
+
+/* Copy the handle's material ids (nx*ny*nz bytes, C order) to host, e.g. to
+ * check a device-built crystal.  No reference counterpart (the reference's
+ * Material.C / P are host arrays already). */
+int phono_download_materials(phono_handle *h, uint8_t *host, size_t bytes);
+
 /* The handle's cudaStream_t (as void*), for callers that record their own
  * CUDA events around phono_step. */
 void *phono_stream(phono_handle *h);
 
-/* Wait for the handle's stream; returns PHONO_ERR_NUMERIC if a recorded
- * surface value was not finite. */
+/* Wait for the handle's stream; returns PHONO_ERR_TIMEOUT if a tile block's
+ * bounded wait for its plane copies ran out (the block flagged it, waited for
+ * the copies it had issued and returned; the state of that step is invalid
+ * and phono_reset clears the flag), PHONO_ERR_NUMERIC if a recorded surface
+ * value was not finite. */
 int phono_sync(phono_handle *h);
+
+/* Test hook for the time-out path above; no reference counterpart.  Every
+ * mbarrier wait of the tile pass gives up after `polls` polls (0: the default
+ * budget, about 0.3 s).  With skip_plane >= 0, every tile block that reads
+ * plane skip_plane arms that plane's barrier but issues no copy for it, so
+ * its wait on it runs out; the next phono_sync returns PHONO_ERR_TIMEOUT.
+ * phono_test_wait_timeout(h, 0, -1) turns it off. */
+int phono_test_wait_timeout(phono_handle *h, int polls, int skip_plane);
 
 /* Copy surface records [first, first+count) to host: count * nx * ny values
  * (float for PHONO_F32K, double otherwise), record r = uz[:, :, 0]

@@ -46,13 +46,10 @@ def available() -> bool:
     return (REF_ROOT / "phonomena" / "simulation" / "base_solver.py").exists()
 
 
-def import_reference():
-    """Import the reference's simulation package with the shims above."""
-    global _mods
-    if _mods is not None:
-        return _mods
-    if not available():
-        raise RuntimeError(f"reference sources not found under {REF_ROOT}")
+def install_shims(h5py_module=None):
+    """Put the stand-ins for the reference's missing imports into sys.modules:
+    ``gui.worker`` (WorkerSignals stub), ``h5py`` (the given module, else the
+    real h5py if present, else an empty module) and ``np.float``."""
     if not hasattr(np, "float"):
         np.float = float  # noqa: NPY001 - the reference still uses the alias
     if "gui.worker" not in sys.modules:
@@ -71,11 +68,23 @@ def import_reference():
         gui.worker = worker
         sys.modules["gui"] = gui
         sys.modules["gui.worker"] = worker
-    if "h5py" not in sys.modules:
+    if h5py_module is not None:
+        sys.modules["h5py"] = h5py_module
+    elif "h5py" not in sys.modules:
         try:
             import h5py  # noqa: F401
         except ImportError:
             sys.modules["h5py"] = types.ModuleType("h5py")
+
+
+def import_reference():
+    """Import the reference's simulation package with the shims above."""
+    global _mods
+    if _mods is not None:
+        return _mods
+    if not available():
+        raise RuntimeError(f"reference sources not found under {REF_ROOT}")
+    install_shims()
     path = str(REF_ROOT / "phonomena")
     if path not in sys.path:
         sys.path.insert(0, path)

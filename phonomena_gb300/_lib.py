@@ -12,7 +12,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_build" / "libphono_gpu.so"
 
 PHONO_OK = 0
 ERRORS = {-1: "PHONO_ERR_ARG", -2: "PHONO_ERR_CUDA", -3: "PHONO_ERR_NOMEM", -4: "PHONO_ERR_STATE",
-          -5: "PHONO_ERR_NUMERIC"}
+          -5: "PHONO_ERR_NUMERIC", -6: "PHONO_ERR_TIMEOUT"}
 
 PRECISIONS = {"f64": 0, "f32k": 1, "f64v": 2}
 SURFACE_MODES = {"reference": 0, "corrected": 1}
@@ -28,7 +28,8 @@ EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done",
            "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
            "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
            "phono_batch_destroy", "phono_set_tiling", "phono_set_segments", "phono_footprint", "phono_set_steps_done",
-           "phono_upload_surface", "phono_set_lattice",
+           "phono_upload_surface", "phono_set_lattice", "phono_set_inclusions", "phono_download_materials",
+           "phono_test_wait_timeout", "phono_time_kernels",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
 
 
@@ -69,6 +70,15 @@ class PhonoLattice(ctypes.Structure):
     _fields_ = [
         ("pitch", ctypes.c_int), ("ncx", ctypes.c_int), ("ncy", ctypes.c_int),
         ("radius", ctypes.c_void_p), ("kind", ctypes.c_void_p), ("depth", ctypes.c_int), ("host", ctypes.c_int),
+    ]
+
+
+class PhonoInclusions(ctypes.Structure):
+    """phono_inclusions of include/phono.h: the reference's inclusion list (Grid.targets)."""
+    _fields_ = [
+        ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p), ("n", ctypes.c_int),
+        ("tx", ctypes.c_void_p), ("ty", ctypes.c_void_p), ("tz", ctypes.c_void_p), ("tr", ctypes.c_void_p),
+        ("id", ctypes.c_void_p), ("inside", ctypes.c_int), ("host", ctypes.c_int),
     ]
 
 
@@ -115,6 +125,10 @@ def load(path: Path | None = None):
         "phono_set_steps_done": (ci, [vp, ci]),
         "phono_upload_surface": (ci, [vp, ci, ci, vp]),
         "phono_set_lattice": (ci, [vp, ctypes.POINTER(PhonoLattice), vp, ci]),
+        "phono_set_inclusions": (ci, [vp, ctypes.POINTER(PhonoInclusions), vp, ci]),
+        "phono_download_materials": (ci, [vp, vp, ctypes.c_size_t]),
+        "phono_test_wait_timeout": (ci, [vp, ci, ci]),
+        "phono_time_kernels": (ci, [vp, ci, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
         "phono_footprint": (ci, [ci, ci, ci, ci, ci, ci, ctypes.POINTER(ctypes.c_size_t)]),
         "phono_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_destroy": (None, [vp]),

@@ -24,6 +24,8 @@ cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, i
 cudaError_t batch_configure_any(int precision, int tj, int* blocks_per_sm);
 cudaError_t launch_lattice_ids(uint8_t* mat, const Geo& g, int pitch, int ncx, int ncy, const double* radius,
                                const uint8_t* kind, int depth, uint8_t host, cudaStream_t st);
+cudaError_t launch_inclusion_ids(uint8_t* mat, const Geo& g, const double* x, const double* y, const double4* incl,
+                                 const int* kend, const uint8_t* id, int n, uint8_t host, cudaStream_t st);
 
 __global__ void advance_step_kernel(int* p, int n) { *p += n; }
 }  // namespace phono
@@ -89,6 +91,8 @@ struct phono_handle {
   int nmat = 0;
   bool timed = false;
   phono_batch* batch = nullptr;  // the batch that steps this handle, if any
+  int wait_polls = 0;            // tile-pass wait budget (0: default)
+  int skip_plane = -1;           // test hook of phono_test_wait_timeout (-1: off)
 };
 
 static long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
@@ -252,15 +256,17 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.faces = h->faces;
   a.err = h->err;
   a.step_end = 0x7fffffff;
+  a.wait_polls = h->wait_polls;
+  a.skip_plane = h->skip_plane;
   return a;
 }
 
-static cudaError_t launch_one(phono_handle* h, int step_off) {
-  if (h->d.precision == PHONO_F64)
-    return launch_step_f64(make_args<double>(h, step_off), h->tj, h->separate_faces, h->stream);
-  if (h->d.precision == PHONO_F64V)
-    return launch_step_f64v(make_args<double>(h, step_off), h->tj, h->separate_faces, h->stream);
-  return launch_step_f32k(make_args<float>(h, step_off), h->tj, h->separate_faces, h->stream);
+// one time step (parts: the handle's form; or 2 tile launch only, 3 face launch only)
+static cudaError_t launch_one(phono_handle* h, int step_off, int parts = -1) {
+  const int form = parts < 0 ? h->separate_faces : parts;
+  if (h->d.precision == PHONO_F64) return launch_step_f64(make_args<double>(h, step_off), h->tj, form, h->stream);
+  if (h->d.precision == PHONO_F64V) return launch_step_f64v(make_args<double>(h, step_off), h->tj, form, h->stream);
+  return launch_step_f32k(make_args<float>(h, step_off), h->tj, form, h->stream);
 }
 
 // Padded device layout: planes -1..nx, rows -1..ny, a KOFF-element front pad
@@ -705,14 +711,74 @@ int phono_step(phono_handle* h, int nsteps) {
   return PHONO_OK;
 }
 
+int phono_time_kernels(phono_handle* h, int nsteps, float* tile_ms, float* face_ms) {
+  if (!h || !tile_ms || !face_ms) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (nsteps < 1) return fail(PHONO_ERR_ARG, "nsteps must be >= 1");
+  if (h->steps_done + nsteps > h->nsrc)
+    return fail(PHONO_ERR_STATE, "not enough source samples: call phono_set_source with max_steps samples");
+  const bool sep = h->separate_faces != 0;
+  std::vector<cudaEvent_t> ev(3 * (size_t)nsteps, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (size_t q = 0; q < ev.size() && e == cudaSuccess; q++) e = cudaEventCreate(&ev[q]);
+  for (int s = 0; s < nsteps && e == cudaSuccess; s++) {
+    e = cudaEventRecord(ev[3 * s], h->stream);
+    if (e == cudaSuccess) e = launch_one(h, s, sep ? 2 : 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3 * s + 1], h->stream);
+    if (e == cudaSuccess && sep) e = launch_one(h, s, 3);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3 * s + 2], h->stream);
+  }
+  if (e == cudaSuccess) {
+    advance_step_kernel<<<1, 1, 0, h->stream>>>(h->step_base, nsteps);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  float t = 0.f, f = 0.f;
+  for (int s = 0; s < nsteps && e == cudaSuccess; s++) {
+    float a = 0.f, b = 0.f;
+    e = cudaEventElapsedTime(&a, ev[3 * s], ev[3 * s + 1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[3 * s + 1], ev[3 * s + 2]);
+    t += a;
+    f += b;
+  }
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("phono_time_kernels: ") + cudaGetErrorString(e));
+  h->steps_done += nsteps;
+  *tile_ms = t;
+  *face_ms = f;
+  return PHONO_OK;
+}
+
 int phono_steps_done(const phono_handle* h) { return h ? h->steps_done : fail(PHONO_ERR_ARG, "handle is NULL"); }
+
+// the device error word of a handle: bit 2 a tile-pass wait ran out, bit 1 a
+// non-finite surface value
+static int device_error(int err) {
+  if (err & 2) return fail(PHONO_ERR_TIMEOUT, "a tile-pass pipeline wait ran out; the state of that step is invalid");
+  if (err & 1) return fail(PHONO_ERR_NUMERIC, "non-finite value in the recorded surface");
+  return PHONO_OK;
+}
 
 int phono_sync(phono_handle* h) {
   if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
   CK(cudaStreamSynchronize(h->stream));
   int err = 0;
   CK(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (err) return fail(PHONO_ERR_NUMERIC, "non-finite value in the recorded surface");
+  return device_error(err);
+}
+
+int phono_test_wait_timeout(phono_handle* h, int polls, int skip_plane) {
+  if (!h) return fail(PHONO_ERR_ARG, "handle is NULL");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  if (polls < 0 || skip_plane < -1 || skip_plane > h->d.nx) return fail(PHONO_ERR_ARG, "polls >= 0, skip_plane in -1..nx");
+  CK(cudaStreamSynchronize(h->stream));
+  h->wait_polls = polls;
+  h->skip_plane = skip_plane;
+  if (h->graph) {  // the hook is a kernel argument baked into the graph
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
   return PHONO_OK;
 }
 
@@ -886,6 +952,114 @@ int phono_set_lattice(phono_handle* h, const phono_lattice* lat, const double* t
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
+  return PHONO_OK;
+}
+
+// z extent of each inclusion as simulation/grid.py:171-174 computes it.  The
+// first inclusion keeps the z nodes with z <= t.z (the float32 depth widened
+// to double).  That line rebinds the loop's `z` to the kept index array, so
+// every later inclusion keeps the positions p of the previous selection with
+// p <= t.z.  With ascending node coordinates every selection is a prefix of
+// the z nodes: kend[t] is its length.
+static std::vector<int> inclusion_z_extents(const double* z, int nz, const float* tz, int n) {
+  std::vector<int> kend(n);
+  int prev = nz;
+  for (int t = 0; t < n; t++) {
+    const double depth = (double)tz[t];
+    int cnt = 0;
+    if (t == 0) {
+      for (int k = 0; k < nz; k++) cnt += z[k] <= depth;
+    } else {
+      for (int p = 0; p < prev; p++) cnt += (double)p <= depth;
+    }
+    kend[t] = cnt;
+    prev = cnt;
+  }
+  return kend;
+}
+
+int phono_set_inclusions(phono_handle* h, const phono_inclusions* inc, const double* table, int nmat) {
+  if (!h || !inc || !table || !inc->x || !inc->y || !inc->z) return fail(PHONO_ERR_ARG, "NULL argument");
+  if (h->batch) return fail(PHONO_ERR_STATE, "handle is in a batch");
+  const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz, n = inc->n;
+  if (n < 0) return fail(PHONO_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!inc->tx || !inc->ty || !inc->tz || !inc->tr)) return fail(PHONO_ERR_ARG, "NULL inclusion array");
+  if (nmat < 1 || nmat > 256) return fail(PHONO_ERR_ARG, "nmat must be in 1..256");
+  if (inc->host < 0 || inc->host >= nmat) return fail(PHONO_ERR_ARG, "host material id out of range");
+  if (!inc->id && (inc->inside < 0 || inc->inside >= nmat)) return fail(PHONO_ERR_ARG, "inside material id out of range");
+  for (int q = 0; q < n; q++)
+    if (inc->id && inc->id[q] >= nmat) return fail(PHONO_ERR_ARG, "inclusion material id out of range");
+  const double* axes[3] = {inc->x, inc->y, inc->z};
+  const int ns[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; a++)
+    for (int q = 0; q < ns[a]; q++) {
+      if (!std::isfinite(axes[a][q])) return fail(PHONO_ERR_ARG, "node coordinates must be finite");
+      if (q > 0 && !(axes[a][q] > axes[a][q - 1])) return fail(PHONO_ERR_ARG, "node coordinates must ascend");
+    }
+  for (int q = 0; q < nmat * PHONO_TABLE_COLS; q++)
+    if (!std::isfinite(table[q])) return fail(PHONO_ERR_ARG, "material table holds a non-finite value");
+  for (int q = 0; q < nmat; q++)
+    if (!(table[q * PHONO_TABLE_COLS + 12] > 0.0)) return fail(PHONO_ERR_ARG, "density must be > 0");
+  const std::vector<int> kend = inclusion_z_extents(inc->z, nz, inc->tz, n);
+  std::vector<double4> incl(n);
+  std::vector<uint8_t> ids(n);
+  for (int q = 0; q < n; q++) {
+    incl[q] = make_double4((double)inc->tx[q], (double)inc->ty[q], (double)inc->tr[q], 0.0);
+    ids[q] = inc->id ? inc->id[q] : (uint8_t)inc->inside;
+  }
+  // the material at node (0, 0, 0), by the kernel's test (its wave speeds set
+  // the absorbing-face coefficients)
+  int id000 = inc->host;
+  for (int q = n - 1; q >= 0; q--) {
+    if (kend[q] < 1) continue;
+    const double dx = inc->x[0] - incl[q].x, dy = inc->y[0] - incl[q].y;
+    if (std::sqrt(dx * dx + dy * dy) < incl[q].z) {
+      id000 = ids[q];
+      break;
+    }
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  // one scratch allocation: coordinates, inclusions, extents, ids
+  const size_t bx = (size_t)nx * 8, by = (size_t)ny * 8, bi = (size_t)n * sizeof(double4), bk = (size_t)n * 4;
+  const size_t total = bx + by + bi + bk + n + 64;
+  char* d = nullptr;
+  CK(cudaMalloc(&d, total));
+  double* dx = (double*)d;
+  double* dy = (double*)(d + bx);
+  double4* di = (double4*)(d + round_up(bx + by, 32));
+  int* dk = (int*)((char*)di + bi);
+  uint8_t* did = (uint8_t*)(dk + n);
+  cudaError_t e = cudaMemcpy(dx, inc->x, bx, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dy, inc->y, by, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(di, incl.data(), bi, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(dk, kend.data(), bk, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(did, ids.data(), n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_inclusion_ids(h->mat, h->g, dx, dy, di, dk, did, n, (uint8_t)inc->host, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("inclusion ids: ") + cudaGetErrorString(e));
+  int rc = upload_table(h, table, nmat, id000);
+  if (rc) return rc;
+  if (h->graph) {  // the absorbing-face coefficients are kernel arguments baked into the graph
+    CK(cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return PHONO_OK;
+}
+
+int phono_download_materials(phono_handle* h, uint8_t* host, size_t bytes) {
+  if (!h || !host) return fail(PHONO_ERR_ARG, "NULL argument");
+  const int nx = h->d.nx, ny = h->d.ny, nz = h->d.nz;
+  if (bytes != (size_t)nx * ny * nz) return fail(PHONO_ERR_ARG, "byte count does not match nx*ny*nz");
+  CK(cudaStreamSynchronize(h->stream));
+  cudaMemcpy3DParms p{};
+  p.srcPtr = make_cudaPitchedPtr(h->mat + h->g.mo0, h->g.msy, h->g.msy, ny + 2);
+  p.dstPtr = make_cudaPitchedPtr((void*)host, nz, nz, ny);
+  p.extent = make_cudaExtent(nz, ny, nx);
+  p.kind = cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy3DAsync(&p, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return PHONO_OK;
 }
 
@@ -1237,7 +1411,8 @@ int phono_batch_sync(phono_batch* b) {
     if (!b->slot[s]) continue;
     int err = 0;
     CK(cudaMemcpy(&err, b->slot[s]->err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) return fail(PHONO_ERR_NUMERIC, "instance " + std::to_string(s) + ": non-finite surface value or stalled pipeline");
+    if (err & 2) return fail(PHONO_ERR_TIMEOUT, "instance " + std::to_string(s) + ": a tile-pass pipeline wait ran out");
+    if (err) return fail(PHONO_ERR_NUMERIC, "instance " + std::to_string(s) + ": non-finite surface value");
   }
   return PHONO_OK;
 }

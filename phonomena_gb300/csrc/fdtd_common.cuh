@@ -112,6 +112,13 @@ struct StepArgs {
   FaceTable faces;
   int* __restrict__ err;  // device error flags: 1 non-finite surface value, 2 pipeline wait timed out
   int step_end;           // global steps >= step_end are skipped (a batched instance's budget)
+  // Bounded waits of the tile pass: polls of an mbarrier before the wait
+  // gives up (0: the default budget, about 0.3 s).  skip_plane >= 0 is a test
+  // hook: blocks arm that plane's barrier but issue no copy for it, so the
+  // wait on it runs out and the time-out path (error bit 2, drain, return)
+  // runs.  -1 in production.
+  int wait_polls;
+  int skip_plane;
 };
 
 // Batched launch: many instances (each a StepArgs in device memory) share one

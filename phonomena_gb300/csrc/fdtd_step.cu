@@ -546,9 +546,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: false if the phase did not complete within the poll budget
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); it++) {
+// bounded wait: false if the phase did not complete within `limit` polls
+// (limit <= 0: 2^22 polls, about 0.3 s with the back-off below)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = 0) {
+  if (limit <= 0) limit = 1 << 22;
+  for (int it = 0; it < limit; it++) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 64) __nanosleep(64);
   }
@@ -678,6 +680,9 @@ cudaError_t configure_step(int tj) {
   }
 }
 
+// separate_faces: 0 one fused launch (face points in extra blocks), 1 the tile
+// launch then the face launch; 2 only the tile launch and 3 only the face
+// launch of the separate form (phono_time_kernels times them apart)
 template <class S, int TJ>
 static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_faces, cudaStream_t st) {
   const int nfaces = a.faces.off[12];
@@ -685,8 +690,9 @@ static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_face
   dim3 block(TK, NT / TK);
   // fused: face points handled by extra blocks of the same launch
   dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + NT - 1) / NT));
-  fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<S, TJ>::bytes(a.nmat), st>>>(a);
-  if (separate_faces && nfaces > 0) fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
+  if (separate_faces != 3) fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<S, TJ>::bytes(a.nmat), st>>>(a);
+  if ((separate_faces == 1 || separate_faces == 3) && nfaces > 0)
+    fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -30,6 +30,18 @@ def footprint(shape, precision="f32k", max_steps=0, record_every=0):
     return int(out.value)
 
 
+def inclusion_columns(targets):
+    """(tx, ty, tz, tr) float32 columns of an inclusion list: a NumPy record
+    array with fields x, y, z, r (the reference's Grid.targets) or a sequence
+    of (x, y, z, r) rows."""
+    t = np.asarray(targets)
+    if t.dtype.names and all(k in t.dtype.names for k in ("x", "y", "z", "r")):
+        t = np.atleast_1d(t)
+        return tuple(np.ascontiguousarray(t[k], dtype=np.float32) for k in ("x", "y", "z", "r"))
+    t = np.asarray(targets, dtype=np.float64).reshape(-1, 4)
+    return tuple(np.ascontiguousarray(t[:, q], dtype=np.float32) for q in range(4))
+
+
 class DeviceSimulation:
     """Device-resident FDTD state behind ``phono_create`` / ``phono_step``.
 
@@ -132,12 +144,45 @@ class DeviceSimulation:
         self._lattice = lat
         self.table = t
 
-    def host_ids(self):
-        """The node material ids on the host (rebuilt from the lattice if they were made on the device)."""
-        if self.mat is None:
-            from .crystal import ids_from_lattice
+    def set_inclusions(self, x, y, z, targets, table, inside=1, host=0, ids=None):
+        """Material ids of the reference's inclusion model built on the device
+        (phono_set_inclusions): node coordinates x, y, z and the inclusion list
+        ``targets`` as the reference's Grid.targets holds it (fields or columns
+        x, y, z, r, stored as float32); ``ids`` optionally gives each inclusion
+        its own material id (default: all ``inside``)."""
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        if (x.size, y.size, z.size) != (self.nx, self.ny, self.nz):
+            raise ValueError("node coordinates do not match the mesh")
+        cols = inclusion_columns(targets)
+        n = cols[0].size
+        idv = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint8)
+        if idv is not None and idv.size != n:
+            raise ValueError("one material id per inclusion")
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 13)
+        d = _lib.PhonoInclusions(x.ctypes.data, y.ctypes.data, z.ctypes.data, n,
+                                 *(c.ctypes.data for c in cols), None if idv is None else idv.ctypes.data,
+                                 int(inside), int(host))
+        check(self._L.phono_set_inclusions(self._h, ctypes.byref(d), t.ctypes.data, t.shape[0]))
+        self.mat = None  # ids live on the device; host_ids() reads them back when asked
+        self._lattice = None
+        self.table = t
 
-            self.mat = ids_from_lattice((self.nx, self.ny, self.nz), self._lattice)
+    def test_wait_timeout(self, polls=0, skip_plane=-1):
+        """Test hook of the tile pass's bounded waits (phono_test_wait_timeout):
+        with skip_plane >= 0 the waits on that plane run out after ``polls``
+        polls and the next sync() raises PHONO_ERR_TIMEOUT; (0, -1) turns it off."""
+        check(self._L.phono_test_wait_timeout(self._h, int(polls), int(skip_plane)))
+
+    def download_materials(self):
+        """The node material ids held on the device, (nx, ny, nz) uint8."""
+        out = np.empty((self.nx, self.ny, self.nz), dtype=np.uint8)
+        check(self._L.phono_download_materials(self._h, out.ctypes.data, out.nbytes))
+        return out
+
+    def host_ids(self):
+        """The node material ids on the host (read back from the device if they were built there)."""
+        if self.mat is None:
+            self.mat = self.download_materials()
         return self.mat
 
     @property
@@ -151,6 +196,13 @@ class DeviceSimulation:
     @property
     def steps_done(self):
         return int(self._L.phono_steps_done(self._h))
+
+    def time_kernels(self, n):
+        """Advance n steps with the tile and face launches timed apart by CUDA
+        events (phono_time_kernels): (tile ms, face ms) summed over the steps."""
+        t, f = ctypes.c_float(), ctypes.c_float()
+        check(self._L.phono_time_kernels(self._h, int(n), ctypes.byref(t), ctypes.byref(f)))
+        return float(t.value), float(f.value)
 
     def last_step_ms(self):
         ms = ctypes.c_float()

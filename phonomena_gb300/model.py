@@ -135,14 +135,20 @@ class Grid:
         self.targets = []
 
     def inclusionIndices(self):
-        """(yx, z) index pairs of nodes inside each cylinder (simulation/grid.py:158-175)."""
+        """(yx, z) index pairs of nodes inside each cylinder (simulation/grid.py:158-175).
+
+        The reference's loop assigns its z selection to the name that held
+        the node coordinates (grid.py:174), so only the first inclusion
+        compares coordinates with its depth; each later one compares the
+        previous selection's positions.  Kept as is: results must match."""
         out = []
         X, Y = np.meshgrid(self.x, self.y)
+        zsel = self.z
         for tx, ty, tz, tr in self.targets:
             R = np.sqrt(np.square(X - np.float32(tx)) + np.square(Y - np.float32(ty)))
             yx = np.array(np.where(R < np.float32(tr))).transpose()
-            zi = np.array(np.where(self.z <= np.float32(tz))).flatten()
-            out.append((yx, zi))
+            zsel = np.array(np.where(zsel <= np.float32(tz))).flatten()
+            out.append((yx, zsel))
         return out
 
     def freezeData(self):
@@ -234,3 +240,26 @@ def solver_inputs(grid, material):
     else:
         ids, table = ids_from_CP(np.asarray(material.C), np.asarray(material.P))
     return spacing, ids, table, float(material.dt)
+
+
+def inclusion_inputs(grid, material):
+    """(spacing dict, table, dt, targets) for building the material ids on the
+    device (phono_set_inclusions) from a Grid with inclusions and a
+    two-material Material, this module's or the reference's: table row 0 is
+    the primary material (host), row 1 the secondary (inclusions).  Only the
+    time step is computed on the host (Material.setTimeStep,
+    simulation/material.py:80-93); the per-node constants of
+    Material.setConstants (material.py:55-63) are not built.  None when the
+    material does not follow that model (ids assigned per node)."""
+    if getattr(material, "_custom", None) is not None:
+        return None
+    if getattr(material, "primary", None) is None or getattr(material, "secondary", None) is None:
+        return None
+    if not hasattr(grid, "targets"):
+        return None
+    material.setTimeStep()
+    spacing = {k: np.ravel(np.asarray(getattr(grid, k), dtype=np.float64)).copy()
+               for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz")}
+    table = np.stack([table_row(material.primary["c"], material.primary["p"]),
+                      table_row(material.secondary["c"], material.secondary["p"])])
+    return spacing, table, float(material.dt), grid.targets

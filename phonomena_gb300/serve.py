@@ -25,6 +25,8 @@ Backends: ``GpuBackend`` (the C ABI) and any object with the same methods
 """
 from __future__ import annotations
 
+import hashlib
+
 import heapq
 import queue
 import threading
@@ -107,11 +109,15 @@ class GpuBackend:
 
     def key(self, p: Prepared):
         """Pool key: what a simulation keeps across requests (mesh, spacing,
-        time step, record layout); materials and source are replaced."""
-        sp = b"".join(np.ascontiguousarray(p.spacing[k], np.float64).tobytes()
-                      for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz"))
+        time step, record layout); materials and source are replaced.  The
+        spacings enter as the SHA-256 digest of their bytes: two meshes share
+        a key only when every spacing value is the same (a pooled handle keeps
+        its spacings and divisor table, so a collision would change results)."""
+        h = hashlib.sha256()
+        for k in ("fdx", "fdy", "fdz", "sdx", "sdy", "sdz"):
+            h.update(np.ascontiguousarray(p.spacing[k], np.float64).tobytes())
         return (tuple(int(v) for v in p.shape), max(self.max_steps, int(p.req.steps)), int(p.req.record_every),
-                float(p.dt), hash(sp))
+                float(p.dt), h.hexdigest())
 
     def footprint(self, shape, steps, record_every):
         from .device import footprint

@@ -125,15 +125,27 @@ def test_output_npz_schema(tmp_path):
     m.update()
     nx, ny, nz = g.shape
     g.ux, g.uy, g.uz = np.zeros((nx - 1, ny, nz)), np.zeros((nx, ny - 1, nz)), np.zeros((nx, ny, nz - 1))
-    s = SimpleNamespace(g=g, m=m, t=10, cfg={"wave": "ricker"}, record_every=2,
-                        surface=np.arange(5 * nx * ny, dtype=np.float64).reshape(5, nx, ny))
+    s = SimpleNamespace(g=g, m=m, t=10, cfg={"wave": "ricker"}, record_every=2, volume=None,
+                        surface=np.arange(5 * nx * ny, dtype=np.float64).reshape(5, nx, ny),
+                        material_ids=lambda: m.ids, material_table=lambda: m.table)
     path = write_results(tmp_path / "out.hdf", s)
     data, attrs = read_results(path)
     assert data["uz"].shape == (nx, ny, 1, 5)
     assert np.array_equal(data["uz"][:, :, 0, 3], s.surface[3])
-    assert attrs["dt_record"] == m.dt * 2
+    assert "ux" not in data and data["ux_final"].shape == (nx - 1, ny, nz)
+    # the time step of the record axis is what analysis.spectrum reads (analysis.py:61-65)
+    assert attrs["dt"] == m.dt * 2 and attrs["dt_step"] == m.dt and attrs["record_every"] == 2
+    assert attrs["steps"] == 5 and attrs["solver_steps"] == 10 and attrs["layout"] == "surface"
+    assert np.asarray(attrs["fdx"]).shape == (nx - 1, 1, 1)  # spectrum reads attrs["fdx"][:, 0, 0] for ux
+    assert data["density"].shape == (nx, ny, nz) and data["material_ids"].shape == (nx, ny, nz)
     for k in ("x", "y", "z", "sdx", "fdz", "steps", "dt", "prim_material", "sec_material", "solver_cfg"):
         assert k in attrs
+    vol = {"ux": np.ones((nx - 1, ny, nz, 3)), "uy": np.ones((nx, ny - 1, nz, 3)), "uz": np.ones((nx, ny, nz - 1, 3))}
+    s.volume, s.record_every = vol, 1
+    data, attrs = read_results(write_results(tmp_path / "vol.hdf", s))
+    assert attrs["layout"] == "volume" and attrs["dt"] == m.dt and attrs["steps"] == 3
+    for k, v in vol.items():
+        assert data[k].shape == v.shape
 
 
 def test_footprint_is_the_padded_layout():
