@@ -21,6 +21,7 @@ def main(argv=None):
     p.add_argument("--precision", default="f32k", choices=["f64", "f32k", "f64v"])
     p.add_argument("--tile-j", type=int, default=8)
     p.add_argument("--x-segment", type=int, default=32)
+    p.add_argument("--x-segments", default="", help="explicit x segment lengths, comma separated (phono_set_segments)")
     p.add_argument("--batch", type=int, default=0, help="run this many crystals of the batching mix instead")
     p.add_argument("--seed", type=int, default=0)
     a = p.parse_args(argv)
@@ -55,12 +56,13 @@ def main(argv=None):
         return 0
 
     cells = tuple(int(c) for c in a.cells.split(","))
+    xs = [int(v) for v in a.x_segments.split(",")] if a.x_segments else a.x_segment
     spec = crystal.CrystalSpec(cells=cells, lattice=16, radius=(0.2, 0.4), depth=10, tungsten_frac=0.25,
                                seed=a.seed, steps=a.steps)
     g, m = crystal.build(spec)
     t0 = time.perf_counter()
     with DeviceSimulation(g.spacing(), m.ids, m.table, m.dt, precision=a.precision, surface_mode="corrected",
-                          max_steps=a.steps, record_every=10, tile_j=a.tile_j, x_segment=a.x_segment) as sim:
+                          max_steps=a.steps, record_every=10, tile_j=a.tile_j, x_segment=xs) as sim:
         sim.set_source(crystal.sin_source(spec.freq, m.dt, a.steps))
         sim.step(a.steps)
         sim.sync()
