@@ -257,7 +257,10 @@ def reference_arm(args, rank, world):
         "e2e": {"value": round(val, 6), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if not args.no_reference_numpy:
-        line["reference_numpy"] = reference_numpy()
+        try:
+            line["reference_numpy"] = reference_numpy()
+        except Exception as e:  # noqa: BLE001 - the port's value stands without it
+            line["reference_numpy"] = {"error": f"{type(e).__name__}: {e}"[:500]}
     print(json.dumps(line), flush=True)
 
 
@@ -767,11 +770,19 @@ def main():
     sim.close()
 
     # ---- the untimed studies of the line: config-3 error table, served latency ----
+    # a failure inside a study is reported in the line instead of losing it
+    def study(fn, *a):
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            torch.cuda.synchronize()
+            return {"error": f"{type(e).__name__}: {e}"[:500]}
+
     prec3 = None
     if not args.no_precision:
         pc = tuple(int(c) for c in args.precision_cells.split(","))
-        prec3 = precision_study(pc, args.precision_steps, rank, torch)
-    served = None if args.no_serve else serve_study(args, rank)
+        prec3 = study(precision_study, pc, args.precision_steps, rank, torch)
+    served = None if args.no_serve else study(serve_study, args, rank)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
