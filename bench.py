@@ -775,7 +775,10 @@ def main():
         try:
             return fn(*a)
         except Exception as e:  # noqa: BLE001
-            torch.cuda.synchronize()
+            try:
+                torch.cuda.synchronize()
+            except Exception:  # noqa: BLE001
+                pass
             return {"error": f"{type(e).__name__}: {e}"[:500]}
 
     prec3 = None
