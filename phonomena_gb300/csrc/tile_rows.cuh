@@ -122,7 +122,9 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
     const int q = p - ibase, sl = q & (NSLOT - 1);
     const bool pw = p >= ib && p < ie;
     mbar_expect_tx(&bars[sl], P::tx_bytes + (pw ? P::pw_bytes : 0u));
-    if (p == a.skip_plane) return;  // test hook: armed, no copy (the wait on it runs out)
+    // test hook (skip_plane >= 0; -1 is off, and plane -1 is a real padding
+    // plane that segment 0 loads): armed, no copy, so the wait on it runs out
+    if (a.skip_plane >= 0 && p == a.skip_plane) return;
     // padded coordinates: k + KOFF, j + 1, i + 1; the u tiles start at k0-KB, j0-1
     tma_load_4d(uring + sl * SU, &maps->tm_u, k0 - KB + Lay<R>::KOFF, j0, p + 1, r.rcur * 3, &bars[sl]);
     tma_load_3d(mring + sl * SM, &maps->tm_mat, k0, j0, p + 1, &bars[sl]);
@@ -613,7 +615,7 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
     if (tid == 0) {
       atomicOr(a.err, 2);
       for (int p = max(ibase, issued - NSLOT + 1); p <= issued; p++) {
-        if (p == a.skip_plane) continue;
+        if (a.skip_plane >= 0 && p == a.skip_plane) continue;
         const int q = p - ibase;
         mbar_wait(&bars[q & (NSLOT - 1)], (q >> 2) & 1);
       }
