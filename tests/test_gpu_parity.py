@@ -376,15 +376,15 @@ def test_device_lattice_ids_equal_host_ids(gpu_lib, cells, a, seed):
 
 
 def test_time_kernels_equals_step(gpu_lib):
-    """phono_time_kernels (the tile and face launches of each step timed apart,
-    no graph) advances the state exactly as phono_step does."""
+    """phono_time_kernels (each step launch between its own CUDA events, no
+    graph) advances the state exactly as phono_step does."""
     d = G.load("config1_void_corrected")
     with device_sim(d) as a, device_sim(d) as b:
         a.step(37)
         tile_ms, face_ms = b.time_kernels(37)
         a.sync()
         b.sync()
-        assert tile_ms > 0 and face_ms > 0 and b.steps_done == 37
+        assert tile_ms > 0 and face_ms >= 0 and b.steps_done == 37
         for key in ("ux", "uy", "uz"):
             assert np.array_equal(a.download(key), b.download(key)), key
         assert np.array_equal(a.read_surface(), b.read_surface())
