@@ -112,19 +112,18 @@ int phono_create(const phono_desc *desc, phono_handle **out);
  * from update_sin / update_ricker (base_solver.py:294-312). */
 int phono_set_source(phono_handle *h, const double *samples, int n);
 
-/* Advance nsteps time steps; one launch per step (its blocks also write the
- * absorbing-face points), replayed from captured CUDA graphs of 12 steps.
- * Replaces the loop body of BaseSolver.run
+/* Advance nsteps time steps; per step a tile launch and a face launch (one
+ * launch when ny == 3), replayed from captured CUDA graphs of 12 steps.  Replaces the loop body of BaseSolver.run
  * (base_solver.py:245-266): source, update_T, update_T_BC, update_u,
  * update_u_BC, time_step.  Asynchronous on the handle's stream. */
 int phono_step(phono_handle *h, int nsteps);
 
 /* Advance nsteps time steps like phono_step, but without the graph and with
- * a CUDA event before and after each launch: *tile_ms = the summed device
- * time of the step launches (one per step: its blocks write the face points
- * too), *face_ms = that of separate face launches (0: there are none).
- * Blocks until done.  Results are those of phono_step.  No reference
- * counterpart (measurement). */
+ * a CUDA event before and after each launch, so that the two kernels of a
+ * step are timed apart: *tile_ms = the summed device time of the tile
+ * launches (the fused launch when ny == 3), *face_ms = that of the face
+ * launches.  Blocks until done.  Results are those of phono_step.  No
+ * reference counterpart (measurement). */
 int phono_time_kernels(phono_handle *h, int nsteps, float *tile_ms, float *face_ms);
 
 /* Global steps completed so far (host-side count of enqueued steps). */
@@ -293,9 +292,9 @@ typedef struct phono_energy_dense {
 int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *stream);
 
 /* Batches: many simulations stepped together.  Every time step is one
- * persistent launch (CTAs pull (instance, tile) work items until none are
- * left; the tiles also write their face points), replayed from a captured
- * CUDA graph.  The reference runs one simulation per solver object
+ * persistent tile launch (CTAs pull (instance, tile) work items until none
+ * are left) and one face launch for all active instances, replayed from a
+ * captured CUDA graph.  The reference runs one simulation per solver object
  * (base_solver.py:245-266) and has no counterpart; the per-instance
  * arithmetic is that of phono_step, bit for bit.  Instances are handles made
  * by phono_create with the batch's precision and tile_j and ny >= 4; each

@@ -1,10 +1,10 @@
 """Many simulations stepped together (phono_batch_* of include/phono.h).
 
 A ``Batch`` holds up to ``capacity`` device simulations of one arithmetic
-scheme and tile height.  Each time step is one persistent launch in which
-the CTAs pull (instance, tile) work items, costliest instances first (the
-tiles also write their face points); chunks of 12 steps are replayed from a
-captured CUDA graph.  Instances keep their own step counters and budgets,
+scheme and tile height.  Each time step is one persistent tile launch in
+which the CTAs pull (instance, tile) work items, costliest instances first,
+plus one face launch for all instances; chunks of 12 steps are replayed from
+a captured CUDA graph.  Instances keep their own step counters and budgets,
 so a batch can hold simulations of different sizes at different points of
 their runs, and instances can join and leave between calls.
 """

@@ -19,7 +19,7 @@ cudaError_t launch_step_f32k(const StepArgs<float>& a, int tj, int n_face_blocks
 cudaError_t configure_step_f64v(int tj);
 cudaError_t launch_step_f64v(const StepArgs<double>& a, int tj, int n_face_blocks, cudaStream_t st);
 cudaError_t launch_energy(const EnergyArgs& a, double2* partial, int nblocks, double* out, cudaStream_t st);
-cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, cudaStream_t st);
+cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st);
 cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, int n, cudaStream_t st);
 cudaError_t batch_configure_any(int precision, int tj, int* blocks_per_sm);
 cudaError_t launch_lattice_ids(uint8_t* mat, const Geo& g, int pitch, int ncx, int ncy, const double* radius,
@@ -258,7 +258,6 @@ static StepArgs<R> make_args(const phono_handle* h, int step_off) {
   a.step_end = 0x7fffffff;
   a.wait_polls = h->wait_polls;
   a.skip_plane = h->skip_plane;
-  a.tile_faces = h->separate_faces ? 1 : 0;
   return a;
 }
 
@@ -1137,8 +1136,10 @@ struct phono_batch {
   char* d_inst = nullptr;
   int2* d_items = nullptr;
   int item_cap = 0;
-  int* d_counts = nullptr;  // work items, active instances
+  int* d_counts = nullptr;  // items, face blocks, face entries, active instances
   unsigned* d_ticket = nullptr;
+  int* d_face_prefix = nullptr;
+  int* d_face_inst = nullptr;
   int* d_active = nullptr;
   std::vector<phono_handle*> slot;
   std::vector<int> remaining;
@@ -1146,7 +1147,7 @@ struct phono_batch {
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false, dirty = true;
-  int grid_tiles = 0;
+  int grid_tiles = 0, grid_faces = 0;
 };
 
 // a handle destroyed while in a batch leaves it (the batch's work list is
@@ -1191,6 +1192,8 @@ static BatchArgs<float> batch_args(const phono_batch* b, int step_off) {
   ba.items = b->d_items;
   ba.counts = b->d_counts;
   ba.ticket = b->d_ticket;
+  ba.face_prefix = b->d_face_prefix;
+  ba.face_inst = b->d_face_inst;
   ba.active = b->d_active;
   ba.step_off = step_off;
   return ba;
@@ -1198,7 +1201,7 @@ static BatchArgs<float> batch_args(const phono_batch* b, int step_off) {
 static_assert(sizeof(BatchArgs<float>) == sizeof(BatchArgs<double>), "batch argument layouts differ");
 static_assert(PHONO_MAX_SEGMENTS == SEG_TABLE, "segment list limit and the kernel table differ");
 
-// work items (costliest instances first) and the active list
+// work items (costliest instances first), face-block prefix, active list
 static int batch_rebuild(phono_batch* b) {
   std::vector<int> act;
   for (int s = 0; s < b->cap; s++)
@@ -1208,10 +1211,16 @@ static int batch_rebuild(phono_batch* b) {
     return cx != cy ? cx > cy : x < y;
   });
   std::vector<int2> items;
+  std::vector<int> prefix, finst;
+  int fb = 0;
   for (int s : act) {
     const phono_handle* h = b->slot[s];
     for (int t = 0; t < h->n_tile; t++) items.push_back(make_int2(s, t));
+    prefix.push_back(fb);
+    finst.push_back(s);
+    fb += (h->faces.off[12] + 255) / 256;
   }
+  prefix.push_back(fb);
   if ((int)items.size() > b->item_cap) {
     int cap = std::max<int>((int)items.size(), 2 * b->item_cap);
     void* p = nullptr;
@@ -1224,11 +1233,14 @@ static int batch_rebuild(phono_batch* b) {
       b->graph = nullptr;
     }
   }
-  int counts[2] = {(int)items.size(), (int)act.size()};
+  int counts[4] = {(int)items.size(), fb, (int)finst.size(), (int)act.size()};
   if (!items.empty())
     CK(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
-  if (!act.empty())
+  CK(cudaMemcpyAsync(b->d_face_prefix, prefix.data(), prefix.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  if (!finst.empty()) {
+    CK(cudaMemcpyAsync(b->d_face_inst, finst.data(), finst.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemcpyAsync(b->d_active, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
   CK(cudaMemcpyAsync(b->d_counts, counts, sizeof counts, cudaMemcpyHostToDevice, b->stream));
   CK(cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned), b->stream));
   CK(cudaStreamSynchronize(b->stream));  // host vectors go out of scope
@@ -1239,7 +1251,7 @@ static int batch_rebuild(phono_batch* b) {
 static cudaError_t batch_launch_steps(phono_batch* b, int first_off, int n) {
   for (int s = 0; s < n; s++) {
     BatchArgs<float> ba = batch_args(b, first_off + s);
-    cudaError_t e = batch_step_any(b->precision, &ba, b->tj, b->grid_tiles, b->stream);
+    cudaError_t e = batch_step_any(b->precision, &ba, b->tj, b->grid_tiles, b->grid_faces, b->stream);
     if (e != cudaSuccess) return e;
   }
   BatchArgs<float> ba = batch_args(b, 0);
@@ -1285,16 +1297,19 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** ou
   BTRYC(cudaEventCreate(&b->ev0));
   BTRYC(cudaEventCreate(&b->ev1));
   BTRY(balloc(b, (void**)&b->d_inst, b->inst_size * capacity));
-  BTRY(balloc(b, (void**)&b->d_counts, sizeof(int) * 2));
+  BTRY(balloc(b, (void**)&b->d_counts, sizeof(int) * 4));
   BTRY(balloc(b, (void**)&b->d_ticket, sizeof(unsigned)));
+  BTRY(balloc(b, (void**)&b->d_face_prefix, sizeof(int) * (capacity + 1)));
+  BTRY(balloc(b, (void**)&b->d_face_inst, sizeof(int) * capacity));
   BTRY(balloc(b, (void**)&b->d_active, sizeof(int) * capacity));
-  BTRYC(cudaMemset(b->d_counts, 0, sizeof(int) * 2));
+  BTRYC(cudaMemset(b->d_counts, 0, sizeof(int) * 4));
   BTRYC(cudaMemset(b->d_ticket, 0, sizeof(unsigned)));
   int bps = 0, dev = 0, nsm = 0;
   BTRYC(batch_configure_any(precision, tile_j, &bps));
   BTRYC(cudaGetDevice(&dev));
   BTRYC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   b->grid_tiles = std::max(1, bps) * nsm;
+  b->grid_faces = 8 * nsm;
 #undef BTRY
 #undef BTRYC
   *out = b;

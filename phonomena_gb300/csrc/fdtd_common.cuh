@@ -119,21 +119,19 @@ struct StepArgs {
   // runs.  -1 in production.
   int wait_polls;
   int skip_plane;
-  // 1: the tile pass writes every face point (x = N, y = 0, y = N and the
-  // z = N points on them) and no face pass runs; 0: the face blocks of the
-  // same launch write them (meshes with ny == 3)
-  int tile_faces;
 };
 
 // Batched launch: many instances (each a StepArgs in device memory) share one
-// persistent launch per step.
+// persistent tile launch and one face launch per step.
 template <class R>
 struct BatchArgs {
   const StepArgs<R>* inst;  // [capacity] per-instance arguments
   const int2* items;        // (instance, tile) work items, costliest first
-  const int* counts;        // [0] work items, [1] active instances
+  const int* counts;        // [0] work items, [1] face blocks, [2] entries of face_prefix
   unsigned* ticket;         // work-item counter; returns to 0 after every launch
-  const int* active;        // [counts[1]] active instances (step-counter update)
+  const int* face_prefix;   // first face block of each listed instance (+ total)
+  const int* face_inst;     // instance of each listed entry
+  const int* active;        // [counts[3]] active instances (step-counter update)
   int step_off;             // offset of this launch inside a captured chunk of steps
 };
 

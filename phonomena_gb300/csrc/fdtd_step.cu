@@ -1,27 +1,27 @@
 // Elastic FDTD step for GB300 (sm_103a).
 //
 // One time step of phonomena's staggered-grid solver
-// (simulation/base_solver.py:245-266) is one launch of fdtd_step_kernel:
+// (simulation/base_solver.py:245-266) is a tile launch and a face launch:
 //
-//  * tile blocks (tile_rows.cuh): a (TJ x 32) tile of the (y, z) plane
-//    marches along x over a segment of planes.  Planes of u (all three
-//    components, 1-node halo), of the material ids and of the pointwise state
-//    of the own points (u_old, or v and the Kahan term) stream into a 4-slot
-//    shared-memory ring through TMA (cp.async.bulk.tensor, completion on an
-//    mbarrier per slot).  Each iteration evaluates the six stresses of the
-//    current plane once (plus the halo stresses the neighbours need) into
+//  * tile blocks (tile_path.cuh, tile_rows.cuh): a (TJ x 32) tile of the
+//    (y, z) plane marches along x over a segment of planes.  Planes of u (all
+//    three components, 1-node halo), of the material ids and of the pointwise
+//    state of the own points (u_old, or v and the Kahan term) stream into a
+//    4-slot shared-memory ring through TMA (cp.async.bulk.tensor, completion
+//    on an mbarrier per slot).  Each iteration evaluates the six stresses of
+//    the current plane once (plus the halo stresses the neighbours need) into
 //    shared memory and writes the new state of the plane.  Stresses are never
-//    written to global memory.
+//    written to global memory.  The tile pass also writes the z = N face
+//    point above every (i, j) that is on no x / y face.
 //
-//  * face points: the x = N, y = 0, y = N and z = N faces
-//    (simulation/base_solver.py:540-554).  The reference applies the faces
-//    one after another, each reading the plane next to it as left by the
-//    earlier faces; the final value of a face point is thus a chain of at
-//    most four face formulas ending at the new value of one interior point
-//    q.  The thread that computes q writes the face points whose chains end
-//    at q (tile_rows.cuh, face_chain), so a step needs no second launch.  For
-//    meshes with ny == 3 extra blocks of the same launch write the face
-//    points instead (face_point), evaluating q from the input state.
+//  * face points (fdtd_face_kernel, a second launch; for ny == 3, extra
+//    blocks of the same launch): the x = N, y = 0, y = N faces and the z = N
+//    points on them (simulation/base_solver.py:540-554).  The reference
+//    applies the faces one after another, each reading the plane next to it
+//    as left by the earlier faces; the final value of a face point is thus a
+//    chain of at most four face formulas ending at the interior value of one
+//    point q.  The face thread walks that chain from q's new value (written
+//    by the tile pass; evaluated from the input state in the one-launch form).
 //
 // Three arithmetic schemes share this structure:
 //  F64  - the reference leapfrog u' = (2u - u_old) + (dt^2/P) * div T with the
@@ -31,8 +31,8 @@
 //         Kahan-compensated displacement sum; explicit fmaf only.
 //  F64V - the F32K scheme in FP64.
 //
-// Batches (batch_step_kernel) run the same tile pass over the (instance,
-// tile) work items of many instances in one persistent launch.
+// Batches (batch_step_kernel and friends) run the same tile pass over the
+// (instance, tile) work items of many instances in one persistent launch.
 #include <cstdio>
 #include "fdtd_common.cuh"
 
@@ -516,6 +516,14 @@ __device__ __forceinline__ void face_point(const StepArgs<typename S::R>& a, con
   if (c == 2 && k == 0) record(a, tt, i, j, val);
 }
 
+// separate face pass: runs after the tile-only step launch on the same stream
+template <class S>
+__global__ void __launch_bounds__(256) fdtd_face_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
+  using R = typename S::R;
+  const int tt = __ldg(a.step_base) + a.step_off;
+  const Roles<R> r = roles<S>(a, tt);
+  face_point<S>(a, r, (R)__ldg(a.src + tt), tt, blockIdx.x * 256 + threadIdx.x, true);
+}
 
 // ---------------------------------------------------------------------------
 // TMA + mbarrier helpers (inline PTX)
@@ -600,6 +608,7 @@ struct RowsPerThread {
   static constexpr int value = (S::kahan && sizeof(typename S::R) == 4 && TJ >= 8) ? 2 : 1;
 };
 
+#include "tile_path.cuh"
 #include "tile_rows.cuh"
 
 // the tile pass of one block: one row per thread or RowsPerThread rows
@@ -607,7 +616,10 @@ template <class S, int TJ>
 __device__ __forceinline__ bool run_tile(const StepArgs<typename S::R>& a, unsigned char* base,
                                          const Roles<typename S::R>& r, const typename S::R s, const int tt,
                                          const int tid, const int b, const StepArgs<typename S::R>* maps) {
-  return tile_block_rows<S, TJ>(a, base, r, s, tt, tid, b, maps);
+  if constexpr (RowsPerThread<S, TJ>::value == 1)
+    return tile_block<S, TJ>(a, base, r, s, tt, tid, b, maps);
+  else
+    return tile_block_rows<S, TJ>(a, base, r, s, tt, tid, b, maps);
 }
 
 // ---------------------------------------------------------------------------
@@ -615,12 +627,12 @@ __device__ __forceinline__ bool run_tile(const StepArgs<typename S::R>& a, unsig
 // ---------------------------------------------------------------------------
 // Resident blocks per SM the register allocation is made for (measured on
 // GB300 for the 256x256x128 crystal and the 64-crystal batch).  FP32: tile
-// height 4, 7 blocks of 128 threads (up to 72 registers); heights 8 and 16
+// height 4, 6 blocks of 128 threads (up to 85 registers); heights 8 and 16
 // (two rows a thread), 4 blocks of 128 or 2 of 256 threads (up to 128
 // registers).  FP64: 16 warps per SM.
 template <class R, int TJ, bool BATCH = false>
 struct MinBlocks {
-  static constexpr int value = sizeof(R) == 8 ? (TJ < 16 ? 16 / TJ : 1) : (TJ == 4 ? 7 : (TJ == 8 ? 4 : 2));
+  static constexpr int value = sizeof(R) == 8 ? (TJ < 16 ? 16 / TJ : 1) : (TJ == 4 ? 6 : (TJ == 8 ? 4 : 2));
 };
 template <class S, int TJ>
 __host__ __device__ constexpr int step_threads() { return TK * TJ / RowsPerThread<S, TJ>::value; }
@@ -668,18 +680,19 @@ cudaError_t configure_step(int tj) {
   }
 }
 
-// separate_faces: 0 one launch of tile blocks and face blocks (ny == 3: the
-// face points are evaluated from the input state by extra blocks); 1 the
-// tile launch alone, whose blocks write the face points (a.tile_faces);
-// 2 the same (the tile launch of phono_time_kernels), 3 nothing (its face
-// launch: there is none)
+// separate_faces: 0 one fused launch (face points in extra blocks), 1 the tile
+// launch then the face launch; 2 only the tile launch and 3 only the face
+// launch of the separate form (phono_time_kernels times them apart)
 template <class S, int TJ>
 static cudaError_t launch_tj(const StepArgs<typename S::R>& a, int separate_faces, cudaStream_t st) {
   const int nfaces = a.faces.off[12];
   constexpr int NT = step_threads<S, TJ>();
   dim3 block(TK, NT / TK);
+  // fused: face points handled by extra blocks of the same launch
   dim3 grid(a.n_tile_blocks + (separate_faces ? 0 : (nfaces + NT - 1) / NT));
   if (separate_faces != 3) fdtd_step_kernel<S, TJ><<<grid, block, SmemPlan<S, TJ>::bytes(a.nmat), st>>>(a);
+  if ((separate_faces == 1 || separate_faces == 3) && nfaces > 0)
+    fdtd_face_kernel<S><<<(nfaces + 255) / 256, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -727,31 +740,50 @@ __global__ void __launch_bounds__(step_threads<S, TJ>(), MinBlocks<typename S::R
   }
 }
 
+template <class S>
+__global__ void __launch_bounds__(256) batch_face_kernel(const __grid_constant__ BatchArgs<typename S::R> ba) {
+  using R = typename S::R;
+  const int n_fb = __ldg(ba.counts + 1), n_ent = __ldg(ba.counts + 2);
+  for (int fb = blockIdx.x; fb < n_fb; fb += gridDim.x) {
+    int lo = 0, hi = n_ent - 1;  // last entry whose first block <= fb
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(ba.face_prefix + mid) <= fb) lo = mid;
+      else hi = mid - 1;
+    }
+    const StepArgs<R>& a = ba.inst[__ldg(ba.face_inst + lo)];
+    const int tt = *a.step_base + ba.step_off;
+    if (tt >= a.step_end) continue;
+    const Roles<R> r = roles<S>(a, tt);
+    face_point<S>(a, r, (R)__ldg(a.src + tt), tt, (fb - __ldg(ba.face_prefix + lo)) * 256 + threadIdx.x, true);
+  }
+}
+
 // advance the step counter of every active instance by n, stopping at its budget
 template <class R>
 __global__ void batch_advance_kernel(const __grid_constant__ BatchArgs<R> ba, int n) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= __ldg(ba.counts + 1)) return;
+  if (q >= __ldg(ba.counts + 3)) return;
   const StepArgs<R>& a = ba.inst[__ldg(ba.active + q)];
   int* c = const_cast<int*>(a.step_base);
   *c = min(*c + n, a.step_end);
 }
 
-// one batched time step: the persistent tile launch (batched instances have
-// ny >= 4, so the tile pass writes their face points)
 template <class S, int TJ>
-static cudaError_t batch_launch_tj(const BatchArgs<typename S::R>& ba, int grid_tiles, cudaStream_t st) {
+static cudaError_t batch_launch_tj(const BatchArgs<typename S::R>& ba, int grid_tiles, int grid_faces,
+                                   cudaStream_t st) {
   batch_step_kernel<S, TJ>
       <<<grid_tiles, dim3(TK, step_threads<S, TJ>() / TK), SmemPlan<S, TJ>::bytes(BATCH_TAB_ROWS), st>>>(ba);
+  batch_face_kernel<S><<<grid_faces, 256, 0, st>>>(ba);
   return cudaGetLastError();
 }
 
 template <class S>
-cudaError_t batch_step(const BatchArgs<typename S::R>& ba, int tj, int grid_tiles, cudaStream_t st) {
+cudaError_t batch_step(const BatchArgs<typename S::R>& ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st) {
   switch (tj) {
-    case 4: return batch_launch_tj<S, 4>(ba, grid_tiles, st);
-    case 8: return batch_launch_tj<S, 8>(ba, grid_tiles, st);
-    case 16: return batch_launch_tj<S, 16>(ba, grid_tiles, st);
+    case 4: return batch_launch_tj<S, 4>(ba, grid_tiles, grid_faces, st);
+    case 8: return batch_launch_tj<S, 8>(ba, grid_tiles, grid_faces, st);
+    case 16: return batch_launch_tj<S, 16>(ba, grid_tiles, grid_faces, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -775,10 +807,10 @@ cudaError_t batch_configure(int tj, int* blocks_per_sm) {
   }
 }
 
-cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, cudaStream_t st) {
-  if (precision == 0) return batch_step<F64>(*(const BatchArgs<double>*)ba, tj, grid_tiles, st);
-  if (precision == 2) return batch_step<F64V>(*(const BatchArgs<double>*)ba, tj, grid_tiles, st);
-  return batch_step<F32K>(*(const BatchArgs<float>*)ba, tj, grid_tiles, st);
+cudaError_t batch_step_any(int precision, const void* ba, int tj, int grid_tiles, int grid_faces, cudaStream_t st) {
+  if (precision == 0) return batch_step<F64>(*(const BatchArgs<double>*)ba, tj, grid_tiles, grid_faces, st);
+  if (precision == 2) return batch_step<F64V>(*(const BatchArgs<double>*)ba, tj, grid_tiles, grid_faces, st);
+  return batch_step<F32K>(*(const BatchArgs<float>*)ba, tj, grid_tiles, grid_faces, st);
 }
 
 cudaError_t batch_advance_any(int precision, const void* ba, int n_active_cap, int n, cudaStream_t st) {

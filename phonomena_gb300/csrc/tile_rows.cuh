@@ -1,21 +1,19 @@
-// Tile pass of the fused step kernel (included by fdtd_step.cu).
+// Tile path with several rows per thread (included by fdtd_step.cu after
+// tile_path.cuh; used where RowsPerThread > 1).
 //
-// A block owns a (TJ x 32) tile of the (y, z) plane and marches along x over
-// planes [ib, ie).  Planes of u (3 components, 1-node halo), material ids and
-// the pointwise state of the own points (u_old, or v and the Kahan terms)
-// arrive by TMA in a 4-slot ring.  A thread owns JR rows of one z column
-// (rows j0 + ty*JR .. + JR-1; JR = RowsPerThread: 2 for FP32 at tile heights
-// 8 and 16, else 1), so the per-plane work that does not depend on the row
-// (ring waits, barriers, slot addresses, x spacings, the plane's range tests)
-// is shared by JR nodes.  Every smem access uses offsets fixed per thread
-// and row (own position Lu / Lm, neighbours at constant distance), the range
-// predicates of the reference's slices are split into per-row (j, k) and
-// per-plane (i) parts computed once, ring values and material ids are carried
-// from plane to plane, and the per-axis spacings live in registers, so the
-// inner loop is the stencil arithmetic plus shared-memory traffic.  The
-// arithmetic goes through the same scheme primitives (tn1, ts, div3, abc,
-// update_value) as the face blocks of the ny == 3 form, operation for
-// operation.  The pass also writes the absorbing-face points (face_chain).
+// The block works as in tile_path.cuh -- a (TJ x 32) tile of the (y, z)
+// plane marching along x, the same TMA ring, stress planes and halo tasks --
+// but a thread owns JR rows of one z column
+// (rows j0 + ty*JR .. + JR-1), so the per-plane work that does not depend on
+// the row (ring waits, barriers, slot addresses, x spacings, the plane's
+// range tests) is shared by JR nodes.  Every smem access uses offsets fixed
+// per thread and row (own position Lu / Lm, neighbours at constant distance),
+// the range predicates of the reference's slices are split into per-row
+// (j, k) and per-plane (i) parts computed once, ring values and material ids
+// are carried from plane to plane, and the per-axis spacings live in
+// registers, so the inner loop is the stencil arithmetic plus shared-memory
+// traffic.  The arithmetic goes through the same scheme primitives (tn1, ts,
+// div3, update_value) as the face path, operation for operation.
 // Included inside namespace phono, after SmemPlan and the scheme primitives.
 #pragma once
 
@@ -100,20 +98,6 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
   const bool zface_xy = k == nz - 2;  // ux, uy: z = N at k = nz-1 (ux: and not the x = N plane)
   const bool zface_z = k == nz - 3;   // uz: z = N at k = nz-2
   const bool rigid = a.bc == 1;
-  // The other face points (on the x = N, y = 0 and y = N faces, and the z = N
-  // points on those faces) are written here too when a.tile_faces is set,
-  // each by the thread that owns the point its chain of face formulas ends
-  // at (see face_chain below).  Rows next to a y face: y = 0 is one row
-  // above row 1 for every component; y = N is one row below row ny-2 for ux
-  // and uz, below row ny-3 for uy (uy has ny-1 rows).
-  const bool tf = a.tile_faces != 0;
-  bool y0r[JR], yNr_xz[JR], yNr_y[JR];
-  #pragma unroll
-  for (int q = 0; q < JR; q++) {
-    y0r[q] = tf && jb + q == 1;
-    yNr_xz[q] = tf && jb + q == ny - 2;
-    yNr_y[q] = tf && jb + q == ny - 3;
-  }
 
   // -------- TMA ring --------
   // pointwise state is read for the planes whose points this block updates
@@ -296,75 +280,15 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
   }
 
   // the surface record this step writes (none: nullptr), at the own column of row jb
-  R* rec = nullptr;   // record of this step at (0, jb)
-  R* recb = nullptr;  // record of this step at (0, 0)
+  R* rec = nullptr;
   if (kz && a.record_every > 0 && (tt + 1) % a.record_every == 0) {
     const int slot = (tt + 1) / a.record_every - 1 - a.rec_base;
-    if (slot >= 0 && slot < a.nrec_cap) {
-      recb = a.surf + ((long long)slot * nx) * ny;
-      rec = recb + jb;
-    }
+    if (slot >= 0 && slot < a.nrec_cap) rec = a.surf + ((long long)slot * nx) * ny + jb;
   }
 
   // element offsets inside one array fit in 32 bits (checked at handle creation)
   const unsigned off_j = (unsigned)(g.o0 + (long long)jb * g.sy + k);  // row r: + r*sy
   const unsigned sxu = (unsigned)g.sx, syu = (unsigned)g.sy;
-
-  // Face points (base_solver.py:540-554) whose chain ends at an own point q
-  // of component c, from q's new value `val`.  The reference applies the
-  // faces in the order x = N, y = 0, y = N, z = N, each reading the plane
-  // next to it as the earlier faces left it; so the final value of a face
-  // point is a chain of face formulas that starts at the new value of the
-  // interior point reached by stepping inward off each face the point lies
-  // on.  Here: the x = N point next to q when q is on the last interior plane
-  // (xl), the y = 0 / y = N points next to q and next to that x = N point
-  // (y0 / yN), and the z = N points above each of them (zl).  Values of q's
-  // plane: uq at q; ym / ymz and yp / ypz at the rows above and below, at k
-  // and k+1.  X: the ring tile of the plane beyond q (the x = N plane), at
-  // component offset co.  The F32K state of a face point is v = c = 0, as in
-  // the face blocks (face_point).
-  auto face_chain = [&](const int c, const int co, const R val, const unsigned off, const int qi, const int jq,
-                        const R uq, const R ym, const R ymz, const R yp, const R ypz, const R* X, const int lu,
-                        const bool xl, const bool y0, const bool yN, const bool zl) {
-    const R cx = c == 0 ? a.abc[0] : a.abc[1], cy0 = c == 1 ? a.abc[3] : a.abc[2];
-    const R cyN = c == 1 ? a.abc[5] : a.abc[4], cz = c == 2 ? a.abc[7] : a.abc[6];
-    auto put = [&](const unsigned o, const R v, const bool surf, const int pi, const int pj) {
-      store_point<S>(r, c, o, v, R(0), R(0));
-      if (c == 2 && surf) {  // uz at z = 0: surface record and the non-finite guard
-        if (recb) recb[(long long)pi * ny + pj] = v;
-        if (!isfinite(v)) atomicOr(a.err, 1);
-      }
-    };
-    auto face = [&](const R coef, const R nbr_new, const R self_old, const R nbr_old) {
-      return rigid ? R(0) : S::abc(coef, nbr_new, self_old, nbr_old);
-    };
-    R vx = R(0);
-    if (xl) {  // (xi, j, k) from q = (xi-1, j, k)
-      vx = face(cx, val, X[co + lu], uq);
-      put(off + sxu, vx, kz, qi + 1, jq);
-      if (zl) put(off + sxu + 1, face(cz, vx, X[co + lu + 1], X[co + lu]), false, 0, 0);
-    }
-    if (y0) {  // (i, 0, k) from (i, 1, k)
-      const R v = face(cy0, val, ym, uq);
-      put(off - syu, v, kz, qi, jq - 1);
-      if (zl) put(off - syu + 1, face(cz, v, ymz, ym), false, 0, 0);
-      if (xl) {
-        const R w = face(cy0, vx, X[co + lu - KW], X[co + lu]);
-        put(off + sxu - syu, w, kz, qi + 1, jq - 1);
-        if (zl) put(off + sxu - syu + 1, face(cz, w, X[co + lu - KW + 1], X[co + lu - KW]), false, 0, 0);
-      }
-    }
-    if (yN) {  // (i, jN, k) from (i, jN-1, k)
-      const R v = face(cyN, val, yp, uq);
-      put(off + syu, v, kz, qi, jq + 1);
-      if (zl) put(off + syu + 1, face(cz, v, ypz, yp), false, 0, 0);
-      if (xl) {
-        const R w = face(cyN, vx, X[co + lu + KW], X[co + lu]);
-        put(off + sxu + syu, w, kz, qi + 1, jq + 1);
-        if (zl) put(off + sxu + syu + 1, face(cz, w, X[co + lu + KW + 1], X[co + lu + KW]), false, 0, 0);
-      }
-    }
-  };
 
   // x spacings of plane p: fdx[p] (T5, T6 at p; ux at p+1) and sdx[p-1]
   // (T1..T3 at p; uy, uz at p), read one plane ahead so that their latency
@@ -492,41 +416,12 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
         sT5[p * PL + h_dst] = v;
       }
     }
-    // ux is updated one plane behind, before the barrier below: it reads
-    // only this thread's own stresses of plane i and the stress planes of
-    // plane i-1 (complete since the previous iteration), and its pointwise
-    // state and face-chain inputs come from the ring slot of plane i-1, which
-    // is refilled after the barrier
-    const int pm = p ^ 1;
-    const bool plane_x = i > ib && i - 1 != nx - 2;  // ux of plane i-1 (not the x = N face)
+    // ux is updated one plane behind: its pointwise state is taken from the
+    // slot of plane i-1 before that slot is refilled
     const R* PWm = pwring + ((i - 1 - ibase) & (NSLOT - 1)) * P::PWS + Lp;  // pointwise, plane i-1
+    Pw<R> pwx[JR];
     #pragma unroll
-    for (int q = 0; q < JR; q++) {
-      const int l = L + q * W, lu = Lu + q * KW;
-      if (plane_x && own_x[q]) {
-        // ux_new(i-1, j, k)   (base_solver.py:441-447, 495-501)
-        const unsigned offm = off_i + (unsigned)q * syu - sxu;
-        R val;
-        if (j_n[q]) {
-          const R* row = tab + 16 * id_c[q];  // P[(i-1)+1, j, k]
-          // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
-          const R dv = S::div3(a.dtab, S::sub(t1c[q], t1m[q]), kz ? a.sp.fdx0 : fdx_im,
-                               S::sub(sT6[pm * PL + l], sT6[pm * PL + l - W]), sb[q],
-                               S::sub(sT5[pm * PL + l], sT5[pm * PL + l - 1]), t123_d);
-          R vn, cn;
-          const Pw<R> pwx{PWm[q * TK], S::kahan ? PWm[3 * P::PWC + q * TK] : R(0)};
-          val = update_value<S>(uxm[q], pwx, dv, row[12], a.dt, vn, cn);
-          store_point<S>(r, 0, offm, val, vn, cn);
-        } else {
-          val = store_stale<S>(r, 0, offm);
-        }
-        if (zface_xy)  // ux on z = N from its inner neighbour (base_solver.py:552)
-          store_point<S>(r, 0, offm + 1, rigid ? R(0) : S::abc(a.abc[6], val, uxm_up[q], uxm[q]), R(0), R(0));
-        if (tf && (i - 1 == nx - 3 || y0r[q] || yNr_xz[q]))
-          face_chain(0, XO, val, offm, i - 1, jb + q, uxm[q], Um[XO + lu - KW], Um[XO + lu - KW + 1],
-                     Um[XO + lu + KW], Um[XO + lu + KW + 1], U0, lu, i - 1 == nx - 3, y0r[q], yNr_xz[q], zface_xy);
-      }
-    }
+    for (int q = 0; q < JR; q++) pwx[q] = Pw<R>{PWm[q * TK], S::kahan ? PWm[3 * P::PWC + q * TK] : R(0)};
     __syncthreads();
     // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
     if (tid == 0 && i - 1 + NSLOT <= plast) {
@@ -535,6 +430,8 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
     }
     const R* PW0 = pwring + ((i - ibase) & (NSLOT - 1)) * P::PWS + Lp;  // pointwise, plane i
     const bool plane_yz = i < ie;                     // uy, uz of plane i belong to this segment
+    const bool plane_x = i > ib && i - 1 != nx - 2;  // ux of plane i-1 (not the x = N face)
+    const int pm = p ^ 1;
     #pragma unroll
     for (int q = 0; q < JR; q++) {
       const int l = L + q * W, lu = Lu + q * KW;
@@ -557,9 +454,6 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           }
           if (zface_xy)  // uy on z = N from its inner neighbour (base_solver.py:553)
             store_point<S>(r, 1, off + 1, rigid ? R(0) : S::abc(a.abc[6], val, U0[YO + lu + 1], uyc[q]), R(0), R(0));
-          if (tf && (i == nx - 2 || y0r[q] || yNr_y[q]))
-            face_chain(1, YO, val, off, i, jb + q, uyc[q], U0[YO + lu - KW], U0[YO + lu - KW + 1], U0[YO + lu + KW],
-                       U0[YO + lu + KW + 1], Up, lu, i == nx - 2, y0r[q], yNr_y[q], zface_xy);
         }
         // uz_new(i, j, k)   (base_solver.py:457-463, 511-516)
         if (own_z[q]) {
@@ -584,10 +478,26 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
           }
           if (zface_z)  // uz on z = N from its inner neighbour (base_solver.py:554)
             store_point<S>(r, 2, off + 1, rigid ? R(0) : S::abc(a.abc[7], val, U0[ZO + lu + 1], uzc[q]), R(0), R(0));
-          if (tf && (i == nx - 2 || y0r[q] || yNr_xz[q]))
-            face_chain(2, ZO, val, off, i, jb + q, uzc[q], U0[ZO + lu - KW], U0[ZO + lu - KW + 1], U0[ZO + lu + KW],
-                       U0[ZO + lu + KW + 1], Up, lu, i == nx - 2, y0r[q], yNr_xz[q], zface_z);
         }
+      }
+      if (plane_x && own_x[q]) {
+        // ux_new(i-1, j, k)   (base_solver.py:441-447, 495-501)
+        const unsigned offm = off - sxu;
+        R val;
+        if (j_n[q]) {
+          const R* row = tab + 16 * id_c[q];  // P[(i-1)+1, j, k]
+          // at k = 0 the T5(k-1) halo entry is 0 (the z = 0 row's "T5 - 0")
+          const R dv = S::div3(a.dtab, S::sub(t1c[q], t1m[q]), kz ? a.sp.fdx0 : fdx_im,
+                               S::sub(sT6[pm * PL + l], sT6[pm * PL + l - W]), sb[q],
+                               S::sub(sT5[pm * PL + l], sT5[pm * PL + l - 1]), t123_d);
+          R vn, cn;
+          val = update_value<S>(uxm[q], pwx[q], dv, row[12], a.dt, vn, cn);
+          store_point<S>(r, 0, offm, val, vn, cn);
+        } else {
+          val = store_stale<S>(r, 0, offm);
+        }
+        if (zface_xy)  // ux on z = N from its inner neighbour (base_solver.py:552)
+          store_point<S>(r, 0, offm + 1, rigid ? R(0) : S::abc(a.abc[6], val, uxm_up[q], uxm[q]), R(0), R(0));
       }
       t1m[q] = t1c[q];
       t5m[q] = t5c[q];

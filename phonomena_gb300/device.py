@@ -198,9 +198,8 @@ class DeviceSimulation:
         return int(self._L.phono_steps_done(self._h))
 
     def time_kernels(self, n):
-        """Advance n steps with a CUDA event around each step launch
-        (phono_time_kernels): (step-launch ms, separate face-launch ms, 0)
-        summed over the steps."""
+        """Advance n steps with the tile and face launches timed apart by CUDA
+        events (phono_time_kernels): (tile ms, face ms) summed over the steps."""
         t, f = ctypes.c_float(), ctypes.c_float()
         check(self._L.phono_time_kernels(self._h, int(n), ctypes.byref(t), ctypes.byref(f)))
         return float(t.value), float(f.value)
