@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libphono_gpu.so"
 SOURCES = ["fdtd_step.cu", "energy.cu", "lattice.cu", "api.cu"]
-HEADERS = ["fdtd_common.cuh", "div_table.cuh", "tile_path.cuh", "tile_rows.cuh"]
+HEADERS = ["fdtd_common.cuh", "div_table.cuh", "tile_rows.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # No implicit FMA anywhere: device code uses explicit _rn intrinsics for the
 # arithmetic whose rounding must match the reference, and the host code that

@@ -3,7 +3,7 @@
 // One time step of phonomena's staggered-grid solver
 // (simulation/base_solver.py:245-266) is a tile launch and a face launch:
 //
-//  * tile blocks (tile_path.cuh, tile_rows.cuh): a (TJ x 32) tile of the
+//  * tile blocks (tile_rows.cuh): a (TJ x 32) tile of the
 //    (y, z) plane marches along x over a segment of planes.  Planes of u (all
 //    three components, 1-node halo), of the material ids and of the pointwise
 //    state of the own points (u_old, or v and the Kahan term) stream into a
@@ -608,7 +608,6 @@ struct RowsPerThread {
   static constexpr int value = (S::kahan && sizeof(typename S::R) == 4 && TJ >= 8) ? 2 : 1;
 };
 
-#include "tile_path.cuh"
 #include "tile_rows.cuh"
 
 // the tile pass of one block: one row per thread or RowsPerThread rows
@@ -616,10 +615,7 @@ template <class S, int TJ>
 __device__ __forceinline__ bool run_tile(const StepArgs<typename S::R>& a, unsigned char* base,
                                          const Roles<typename S::R>& r, const typename S::R s, const int tt,
                                          const int tid, const int b, const StepArgs<typename S::R>* maps) {
-  if constexpr (RowsPerThread<S, TJ>::value == 1)
-    return tile_block<S, TJ>(a, base, r, s, tt, tid, b, maps);
-  else
-    return tile_block_rows<S, TJ>(a, base, r, s, tt, tid, b, maps);
+  return tile_block_rows<S, TJ>(a, base, r, s, tt, tid, b, maps);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,19 +1,20 @@
-// Tile path with several rows per thread (included by fdtd_step.cu after
-// tile_path.cuh; used where RowsPerThread > 1).
+// Tile pass of the fused step kernel (included by fdtd_step.cu).
 //
-// The block works as in tile_path.cuh -- a (TJ x 32) tile of the (y, z)
-// plane marching along x, the same TMA ring, stress planes and halo tasks --
-// but a thread owns JR rows of one z column
-// (rows j0 + ty*JR .. + JR-1), so the per-plane work that does not depend on
-// the row (ring waits, barriers, slot addresses, x spacings, the plane's
-// range tests) is shared by JR nodes.  Every smem access uses offsets fixed
-// per thread and row (own position Lu / Lm, neighbours at constant distance),
-// the range predicates of the reference's slices are split into per-row
-// (j, k) and per-plane (i) parts computed once, ring values and material ids
-// are carried from plane to plane, and the per-axis spacings live in
-// registers, so the inner loop is the stencil arithmetic plus shared-memory
-// traffic.  The arithmetic goes through the same scheme primitives (tn1, ts,
-// div3, update_value) as the face path, operation for operation.
+// A block owns a (TJ x 32) tile of the (y, z) plane and marches along x over
+// planes [ib, ie).  Planes of u (3 components, 1-node halo), material ids and
+// the pointwise state of the own points (u_old, or v and the Kahan terms)
+// arrive by TMA in a 4-slot ring.  A thread owns JR rows of one z column
+// (rows j0 + ty*JR .. + JR-1; JR = RowsPerThread: 2 for FP32 at tile heights
+// 8 and 16, else 1), so the per-plane work that does not depend on the row
+// (ring waits, barriers, slot addresses, x spacings, the plane's range tests)
+// is shared by JR nodes.  Every smem access uses offsets fixed per thread
+// and row (own position Lu / Lm, neighbours at constant distance), the range
+// predicates of the reference's slices are split into per-row (j, k) and
+// per-plane (i) parts computed once, ring values and material ids are carried
+// from plane to plane, and the per-axis spacings live in registers, so the
+// inner loop is the stencil arithmetic plus shared-memory traffic.  The
+// arithmetic goes through the same scheme primitives (tn1, ts, div3,
+// update_value) as the face path, operation for operation.
 // Included inside namespace phono, after SmemPlan and the scheme primitives.
 #pragma once
 
