@@ -423,6 +423,12 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
     Pw<R> pwx[JR];
     #pragma unroll
     for (int q = 0; q < JR; q++) pwx[q] = Pw<R>{PWm[q * TK], S::kahan ? PWm[3 * P::PWC + q * TK] : R(0)};
+    // The slot of plane i-1 is refilled by a TMA copy (async proxy) that
+    // thread 0 issues after the barrier.  A barrier orders shared-memory
+    // accesses of the block's threads only: without this proxy fence a read
+    // of the slot issued above may still be pending when the copy lands
+    // (seen under heavy HBM traffic from other work on the GPU).
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     // plane i-1 is no longer read: refill its slot with plane i-1+NSLOT
     if (tid == 0 && i - 1 + NSLOT <= plast) {
@@ -533,7 +539,9 @@ __device__ __forceinline__ bool tile_block_rows(const StepArgs<typename S::R>& a
     }
   }
   // every issued plane has been waited for; the barriers may be set up
-  // again by the next tile of a persistent block
+  // again by the next tile of a persistent block, whose copies write the
+  // ring: order this thread's reads of it first (as before a refill)
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
   if (tid == 0)
     for (int q = 0; q < NSLOT; q++) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[q])) : "memory");
