@@ -50,6 +50,8 @@ def parse():
                         "launch; serve: Poisson request stream; precision: 1024x1024x256 FP32K vs FP64 error")
     p.add_argument("--fdtd-steps", type=int, default=None)
     p.add_argument("--instances", type=int, default=64)
+    p.add_argument("--batch-streams", type=int, default=64,
+                   help="batch workload: worker streams of the streams scheme (0: the persistent scheme only)")
     p.add_argument("--requests", type=int, default=2000, help="serve: FP32K requests")
     p.add_argument("--rate", type=float, default=0.0, help="serve: FP32K arrivals per second (0: 70%% load)")
     p.add_argument("--requests-f64", type=int, default=40, help="serve: plain FP64 requests")
@@ -266,10 +268,12 @@ def reference_arm(args, rank, world):
 
 def bench_batch(args, rank, world, local, torch, dist):
     """64 uneven seeded crystals (sizes {64..192}^2 x {32..96} cells, a in
-    {8,12,16}, f ~ U[20, 60] MHz), 1500 steps each, FP32 Kahan, in one
-    persistent launch per time step with a graph-captured step loop; tile
-    height and per-instance x segments from the batch autotuner.  One bench
-    step = the whole batch from the zero state to its last step."""
+    {8,12,16}, f ~ U[20, 60] MHz), 1500 steps each, FP32 Kahan, with a
+    graph-captured step loop, in both batch schemes: one persistent tile
+    launch per time step, and every instance's own kernels on worker streams;
+    tile height and per-instance x segments from the batch autotuner for
+    each.  The faster scheme is the line's value.  One bench step = the whole
+    batch from the zero state to its last step."""
     from phonomena_gb300 import autotune, crystal
     from phonomena_gb300.batch import Batch
     from phonomena_gb300.device import DeviceSimulation
@@ -301,24 +305,37 @@ def bench_batch(args, rank, world, local, torch, dist):
             b.remove(q)
         return ms
 
-    tj, segs = autotune.tune_batch(shapes, "f32k")
-    sims = make("f32k", tj, segs)
-    batch = Batch(len(sims), precision="f32k", tile_j=tj)
-    for _ in range(args.warmup):
-        run_once(batch, sims)
-    torch.cuda.synchronize()
-    if dist is not None:
-        dist.barrier()
+    schemes = {"persistent": 0}
+    if args.batch_streams > 0:
+        schemes["streams"] = args.batch_streams
+    timed = {}
     bus = getattr(torch.cuda.get_device_properties(local), "pci_bus_id", "")
-    with ClockSampler(bus) as clk:
-        times = [run_once(batch, sims) for _ in range(args.steps)]
-    ms = sum(times)
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    clocks = clk.summary()
-    value = world * node_sum * S * args.steps / (ms / 1e3) / 1e9
+    for name, streams in schemes.items():
+        tj, segs = autotune.tune_batch(shapes, "f32k", streams=streams)
+        sims = make("f32k", tj, segs)
+        batch = Batch(len(sims), precision="f32k", tile_j=tj, streams=streams)
+        for _ in range(args.warmup):
+            run_once(batch, sims)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        with ClockSampler(bus) as clk:
+            times = [run_once(batch, sims) for _ in range(args.steps)]
+        ms = sum(times)
+        if dist is not None:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        timed[name] = dict(ms=ms, tj=tj, segs=segs, sims=sims, batch=batch, streams=streams, clocks=clk.summary(),
+                           value=world * node_sum * S * args.steps / (ms / 1e3) / 1e9)
+    scheme = min(timed, key=lambda k: timed[k]["ms"])
+    for name, t in timed.items():
+        if name != scheme:
+            t["batch"].close()
+            for s_ in t["sims"]:
+                s_.close()
+    best = timed[scheme]
+    ms, tj, segs, sims, batch, clocks, value = (best[k] for k in ("ms", "tj", "segs", "sims", "batch", "clocks", "value"))
     surf32 = [s.read_surface().astype(np.float64) for s in sims]
 
     # the same instances one after another, each alone on its own handle
@@ -372,9 +389,9 @@ def bench_batch(args, rank, world, local, torch, dist):
     # error, and the energy growth that marks an instance whose reference
     # scheme is unstable (exponential growth amplifies every rounding
     # difference, so its FP32/FP64 difference says nothing about FP32)
-    tj64, segs64 = autotune.tune_batch(shapes, "f64", steps=4, tile_js=(8, 16))
+    tj64, segs64 = autotune.tune_batch(shapes, "f64", steps=4, tile_js=(8, 16), streams=best["streams"])
     sims64 = make("f64", tj64, segs64)
-    b64 = Batch(len(sims64), precision="f64", tile_j=tj64)
+    b64 = Batch(len(sims64), precision="f64", tile_j=tj64, streams=best["streams"])
     slots = [b64.add(s, S) for s in sims64]
     half = S // 2
     b64.step(half)
@@ -399,7 +416,7 @@ def bench_batch(args, rank, world, local, torch, dist):
     launch_ms = ms / (args.steps * S)
     hbm_peak, peak_kind = measured_peaks()
     achieved = BYTES_PER_NODE * node_sum / (launch_ms / 1e3) / 1e9
-    tpn = traffic_per_node("batch_step_kernel_f32k")
+    tpn = traffic_per_node("batch_step_kernel_f32k" if scheme == "persistent" else "fdtd_step_kernel_f32k_batch")
     if rank == 0:
         line = {
             "metric": "Gcell-updates/s", "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": world,
@@ -407,11 +424,14 @@ def bench_batch(args, rank, world, local, torch, dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded crystals)",
             "config": {"workload": f"batch of {len(specs)} uneven crystals ({node_sum} nodes in all), {S} time steps "
-                                   "each, one persistent launch per time step, graph-captured step loop, FP32 Kahan",
-                       "instances": len(specs), "nodes": node_sum, "fdtd_steps": S,
-                       "tile_j": tj, "x_segment_by_instance": segs,
+                                   f"each, {scheme} batch scheme, graph-captured step loop, FP32 Kahan",
+                       "instances": len(specs), "nodes": node_sum, "fdtd_steps": S, "scheme": scheme,
+                       "worker_streams": best["streams"], "tile_j": tj, "x_segment_by_instance": segs,
                        "l2": f"inputs larger than L2 (state {node_sum * 72 / 1e9:.1f} GB)",
                        "parallelism": f"replicas x{world}"},
+            "schemes": {k: {"value": round(t["value"], 4), "unit": "Gcell-updates/s",
+                            "ms_per_step": round(t["ms"] / args.steps, 3), "tile_j": t["tj"],
+                            "x_segments": sorted(set(map(str, t["segs"])))} for k, t in timed.items()},
             "sequential": {"value": round(world * node_sum * S / (seq_ms / 1e3) / 1e9, 4), "unit": "Gcell-updates/s",
                            "ms": round(seq_ms, 3), "speedup_batch_over_sequential":
                                round(seq_ms / (ms / args.steps), 3), "bit_identical_to_batch": bool(same)},
@@ -431,12 +451,16 @@ def bench_batch(args, rank, world, local, torch, dist):
                          "traffic": (round(tpn * node_sum) if tpn else None),
                          "algorithmic_bytes_per_launch": BYTES_PER_NODE * node_sum,
                          "avg_launch_ms": round(launch_ms, 5),
-                         "launch_timing": "one time step = persistent tile launch + batched face launch "
-                                          "(+1/12 counter update); the whole step is charged to the stencil kernel"},
+                         "launch_timing": ("one time step = persistent tile launch + batched face launch "
+                                           "(+1/12 counter update)" if scheme == "persistent" else
+                                           "one time step = every instance's tile and face launches on the worker "
+                                           "streams (+1/12 counter update)")
+                                          + "; the whole step is charged to the stencil kernel"},
             "cpu_baseline": None,
             "e2e": {"value": round(e2e, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": graph_launches(S, True) * args.steps,
+            "gpu_launches": (graph_launches(S, True) if scheme == "persistent"
+                             else len(specs) * 2 * S + -(-S // GRAPH_CHUNK)) * args.steps,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -297,14 +297,25 @@ int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *str
  * captured CUDA graph.  The reference runs one simulation per solver object
  * (base_solver.py:245-266) and has no counterpart; the per-instance
  * arithmetic is that of phono_step, bit for bit.  Instances are handles made
- * by phono_create with the batch's precision and tile_j and ny >= 4; each
- * keeps its own x_segment.  While a handle is in a batch, phono_step,
+ * by phono_create with the batch's precision and ny >= 4 (and the batch's
+ * tile_j in the persistent scheme); each keeps its own x segments.  While a handle is in a batch, phono_step,
  * phono_reset, phono_set_materials, phono_upload and phono_set_tiling on it
  * return PHONO_ERR_STATE; call phono_batch_sync before reading it.  A handle
  * destroyed while in a batch leaves the batch. */
 typedef struct phono_batch phono_batch;
 
 int phono_batch_create(int capacity, int precision, int tile_j, phono_batch **out);
+/* Launch scheme of an empty batch (PHONO_ERR_STATE once it holds an
+ * instance).  PHONO_BATCH_PERSISTENT (the default): the persistent tile
+ * launch above, every instance at the batch's tile_j.  PHONO_BATCH_STREAMS:
+ * every instance runs its own step kernels (those of phono_step, with its own
+ * tile_j and x segments) on one of `streams` worker streams (1..256), so that
+ * instances run side by side; a step is done when every worker stream is.
+ * The graph of 12 steps is captured again whenever the set of active
+ * instances changes.  Results are those of phono_step in both schemes. */
+#define PHONO_BATCH_PERSISTENT 0
+#define PHONO_BATCH_STREAMS 1
+int phono_batch_set_mode(phono_batch *b, int mode, int streams);
 /* Attach h for nsteps more steps; returns the slot (>= 0) or an error code. */
 int phono_batch_add(phono_batch *b, phono_handle *h, int nsteps);
 int phono_batch_remove(phono_batch *b, int slot);

@@ -15,6 +15,7 @@ ERRORS = {-1: "PHONO_ERR_ARG", -2: "PHONO_ERR_CUDA", -3: "PHONO_ERR_NOMEM", -4: 
           -5: "PHONO_ERR_NUMERIC", -6: "PHONO_ERR_TIMEOUT"}
 
 PRECISIONS = {"f64": 0, "f32k": 1, "f64v": 2}
+BATCH_PERSISTENT, BATCH_STREAMS = 0, 1  # phono_batch_set_mode
 SURFACE_MODES = {"reference": 0, "corrected": 1}
 BCS = {"absorbing": 0, "reference": 0, "rigid": 1}
 SOURCE_MODES = {"line": 0, "wall": 1}
@@ -27,7 +28,7 @@ EXPORTS = ["phono_create", "phono_set_source", "phono_step", "phono_steps_done",
            "phono_read_surface", "phono_download", "phono_upload", "phono_elem_size", "phono_energy",
            "phono_energy_static", "phono_batch_create", "phono_batch_add", "phono_batch_remove",
            "phono_batch_remaining", "phono_batch_step", "phono_batch_sync", "phono_batch_last_step_ms",
-           "phono_batch_destroy", "phono_set_tiling", "phono_set_segments", "phono_footprint", "phono_set_steps_done",
+           "phono_batch_destroy", "phono_batch_set_mode", "phono_set_tiling", "phono_set_segments", "phono_footprint", "phono_set_steps_done",
            "phono_upload_surface", "phono_set_lattice", "phono_set_inclusions", "phono_download_materials",
            "phono_test_wait_timeout", "phono_time_kernels",
            "phono_last_step_ms", "phono_destroy", "phono_last_error", "phono_abi_version"]
@@ -120,6 +121,7 @@ def load(path: Path | None = None):
         "phono_batch_sync": (ci, [vp]),
         "phono_batch_last_step_ms": (ci, [vp, ctypes.POINTER(ctypes.c_float)]),
         "phono_batch_destroy": (None, [vp]),
+        "phono_batch_set_mode": (ci, [vp, ci, ci]),
         "phono_set_tiling": (ci, [vp, ci, ci]),
         "phono_set_segments": (ci, [vp, ci, vp, ci]),
         "phono_set_steps_done": (ci, [vp, ci]),

@@ -166,16 +166,18 @@ def _batch_key(precision, shapes):
     return f"batch:{precision}:{len(shapes)}:{h}:{_device_name()}"
 
 
-def tune_batch(shapes, precision="f32k", steps=24, tile_js=TILE_J, use_cache=True, verbose=False):
+def tune_batch(shapes, precision="f32k", steps=24, tile_js=TILE_J, use_cache=True, verbose=False, streams=0):
     """Tile height of a batch and the x segment of each instance.
 
     shapes: mesh node counts (nx, ny, nz) of the instances, in batch order.
+    streams: 0 times the persistent scheme, W > 0 the streams scheme on W
+    worker streams (every instance at the chosen tile height).
     Returns (tile_j, [x_segment per instance]).
     """
     from .batch import Batch
 
     shapes = [tuple(int(v) for v in s) for s in shapes]
-    key = _batch_key(precision, shapes) + ":" + ",".join(map(str, tile_js))
+    key = _batch_key(precision, shapes) + ":" + ",".join(map(str, tile_js)) + (f":streams{streams}" if streams else "")
     if use_cache:
         hit = _load().get(key)
         if hit:
@@ -191,7 +193,7 @@ def tune_batch(shapes, precision="f32k", steps=24, tile_js=TILE_J, use_cache=Tru
     def time_mix(tj, seg_by_nx):
         for sim in sims:
             sim.set_tiling(tj, seg_by_nx[sim.nx])
-        with Batch(len(sims), precision=precision, tile_j=tj) as b:
+        with Batch(len(sims), precision=precision, tile_j=tj, streams=streams) as b:
             for sim in sims:
                 b.add(sim, steps + 12)
             b.step(12)  # work list upload, graph capture
@@ -200,7 +202,7 @@ def tune_batch(shapes, precision="f32k", steps=24, tile_js=TILE_J, use_cache=Tru
             ms = b.last_step_ms() / steps
         log.append([tj, {str(k): v for k, v in seg_by_nx.items()}, round(ms, 5)])
         if verbose:
-            print(f"autotune batch tile_j={tj} x_segment={seg_by_nx}: {ms:.4f} ms/step")
+            print(f"autotune batch streams={streams} tile_j={tj} x_segment={seg_by_nx}: {ms:.4f} ms/step")
         return ms
 
     try:

@@ -1,12 +1,21 @@
 """Many simulations stepped together (phono_batch_* of include/phono.h).
 
 A ``Batch`` holds up to ``capacity`` device simulations of one arithmetic
-scheme and tile height.  Each time step is one persistent tile launch in
-which the CTAs pull (instance, tile) work items, costliest instances first,
-plus one face launch for all instances; chunks of 12 steps are replayed from
-a captured CUDA graph.  Instances keep their own step counters and budgets,
-so a batch can hold simulations of different sizes at different points of
-their runs, and instances can join and leave between calls.
+scheme.  Two launch schemes:
+
+* persistent (``streams=0``, the default): every instance at the batch's
+  tile height; each time step is one persistent tile launch in which the
+  CTAs pull (instance, tile) work items, costliest instances first, plus one
+  face launch for all instances;
+* streams (``streams=W``): every instance runs its own step kernels, with
+  its own tile height and x segments, on one of W worker streams, so that
+  the instances' launches run side by side on the GPU.
+
+Chunks of 12 steps are replayed from a captured CUDA graph (in the streams
+scheme captured again when the set of active instances changes).  Instances
+keep their own step counters and budgets, so a batch can hold simulations of
+different sizes at different points of their runs, and instances can join
+and leave between calls.  Results are those of stepping each alone.
 """
 from __future__ import annotations
 
@@ -17,14 +26,22 @@ from ._lib import check
 
 
 class Batch:
-    def __init__(self, capacity, precision="f32k", tile_j=8):
+    def __init__(self, capacity, precision="f32k", tile_j=8, streams=0):
         L = _lib.load()
         self._L = L
         self.precision = precision
         self.tile_j = int(tile_j)
+        self.streams = int(streams)
         b = ctypes.c_void_p()
         check(L.phono_batch_create(int(capacity), _lib.PRECISIONS[precision], self.tile_j, ctypes.byref(b)))
         self._b = b
+        if self.streams:
+            try:
+                check(L.phono_batch_set_mode(b, _lib.BATCH_STREAMS, self.streams))
+            except Exception:
+                L.phono_batch_destroy(b)
+                self._b = None
+                raise
         self._members = {}  # slot -> DeviceSimulation (kept alive while in the batch)
 
     def add(self, sim, nsteps):

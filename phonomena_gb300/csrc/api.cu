@@ -1148,6 +1148,12 @@ struct phono_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false, dirty = true;
   int grid_tiles = 0, grid_faces = 0;
+  int streams = 0;  // PHONO_BATCH_STREAMS: per-instance launches on this many worker streams
+  std::vector<cudaStream_t> workers;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  std::vector<int> order;     // active slots, costliest first
+  std::vector<int> step_end;  // per slot: the instance's budget end
 };
 
 // a handle destroyed while in a batch leaves it (the batch's work list is
@@ -1171,6 +1177,9 @@ static void batch_release(phono_batch* b) {
   for (void* p : b->allocs) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaStream_t w : b->workers) cudaStreamDestroy(w);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -1221,6 +1230,11 @@ static int batch_rebuild(phono_batch* b) {
     fb += (h->faces.off[12] + 255) / 256;
   }
   prefix.push_back(fb);
+  b->order = act;
+  if (b->streams && b->graph) {  // the captured launches name the old instances
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   if ((int)items.size() > b->item_cap) {
     int cap = std::max<int>((int)items.size(), 2 * b->item_cap);
     void* p = nullptr;
@@ -1248,7 +1262,38 @@ static int batch_rebuild(phono_batch* b) {
   return PHONO_OK;
 }
 
+// one step of instance s on stream st, with the handle's own kernels and tiles
+static cudaError_t chain_launch(phono_batch* b, int s, int step_off, cudaStream_t st) {
+  phono_handle* h = b->slot[s];
+  if (h->d.precision == PHONO_F32K) {
+    StepArgs<float> a = make_args<float>(h, step_off);
+    a.step_end = b->step_end[s];
+    return launch_step_f32k(a, h->tj, h->separate_faces, st);
+  }
+  StepArgs<double> a = make_args<double>(h, step_off);
+  a.step_end = b->step_end[s];
+  return h->d.precision == PHONO_F64 ? launch_step_f64(a, h->tj, h->separate_faces, st)
+                                     : launch_step_f64v(a, h->tj, h->separate_faces, st);
+}
+
+// n steps of every active instance.  Streams scheme: instance q (costliest
+// first) on worker q mod W, forked from and joined back into the batch stream
+// with events (in a graph capture, the same events make the graph's edges).
 static cudaError_t batch_launch_steps(phono_batch* b, int first_off, int n) {
+  if (b->streams) {
+    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    const int nw = std::min<int>((int)b->order.size(), b->streams);
+    for (int w = 0; w < nw && e == cudaSuccess; w++) e = cudaStreamWaitEvent(b->workers[w], b->fork, 0);
+    for (int q = 0; q < (int)b->order.size() && e == cudaSuccess; q++)
+      for (int s = 0; s < n && e == cudaSuccess; s++) e = chain_launch(b, b->order[q], first_off + s, b->workers[q % nw]);
+    for (int w = 0; w < nw && e == cudaSuccess; w++) {
+      e = cudaEventRecord(b->joins[w], b->workers[w]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[w], 0);
+    }
+    if (e != cudaSuccess) return e;
+    BatchArgs<float> ba = batch_args(b, 0);
+    return batch_advance_any(b->precision, &ba, b->cap, n, b->stream);
+  }
   for (int s = 0; s < n; s++) {
     BatchArgs<float> ba = batch_args(b, first_off + s);
     cudaError_t e = batch_step_any(b->precision, &ba, b->tj, b->grid_tiles, b->grid_faces, b->stream);
@@ -1275,6 +1320,7 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** ou
   b->inst_size = precision == PHONO_F32K ? sizeof(StepArgs<float>) : sizeof(StepArgs<double>);
   b->slot.assign(capacity, nullptr);
   b->remaining.assign(capacity, 0);
+  b->step_end.assign(capacity, 0);
 #define BTRY(x)              \
   do {                       \
     int r_ = (x);            \
@@ -1316,11 +1362,42 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** ou
   return PHONO_OK;
 }
 
+int phono_batch_set_mode(phono_batch* b, int mode, int streams) {
+  if (!b) return fail(PHONO_ERR_ARG, "batch is NULL");
+  if (mode != PHONO_BATCH_PERSISTENT && mode != PHONO_BATCH_STREAMS) return fail(PHONO_ERR_ARG, "unknown batch mode");
+  if (mode == PHONO_BATCH_STREAMS && (streams < 1 || streams > 256))
+    return fail(PHONO_ERR_ARG, "streams must be in 1..256");
+  for (phono_handle* h : b->slot)
+    if (h) return fail(PHONO_ERR_STATE, "the launch scheme of a batch is set while it is empty");
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  const int want = mode == PHONO_BATCH_STREAMS ? streams : 0;
+  if (!b->fork && want) CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  while ((int)b->workers.size() < want) {  // worker streams are kept for the batch's lifetime
+    cudaStream_t w = nullptr;
+    cudaEvent_t j = nullptr;
+    CK(cudaStreamCreateWithFlags(&w, cudaStreamNonBlocking));
+    cudaError_t e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      cudaStreamDestroy(w);
+      return fail(PHONO_ERR_CUDA, std::string("cudaEventCreateWithFlags: ") + cudaGetErrorString(e));
+    }
+    b->workers.push_back(w);
+    b->joins.push_back(j);
+  }
+  b->streams = want;
+  b->dirty = true;
+  return PHONO_OK;
+}
+
 int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
   if (!b || !h) return fail(PHONO_ERR_ARG, "NULL argument");
   if (h->batch) return fail(PHONO_ERR_ARG, h->batch == b ? "handle already in the batch" : "handle is in another batch");
   if (h->d.precision != b->precision) return fail(PHONO_ERR_ARG, "handle precision differs from the batch");
-  if (h->tj != b->tj) return fail(PHONO_ERR_ARG, "handle tile_j differs from the batch");
+  if (!b->streams && h->tj != b->tj) return fail(PHONO_ERR_ARG, "handle tile_j differs from the batch");
   if (!h->separate_faces) return fail(PHONO_ERR_ARG, "batched instances need ny >= 4");
   if (h->nmat > BATCH_TAB_ROWS)
     return fail(PHONO_ERR_ARG, "batched instances hold at most " + std::to_string(BATCH_TAB_ROWS) + " materials");
@@ -1345,6 +1422,7 @@ int phono_batch_add(phono_batch* b, phono_handle* h, int nsteps) {
   }
   b->slot[s] = h;
   b->remaining[s] = nsteps;
+  b->step_end[s] = h->steps_done + nsteps;
   b->dirty = true;
   h->batch = b;
   return s;

@@ -521,6 +521,7 @@ template <class S>
 __global__ void __launch_bounds__(256) fdtd_face_kernel(const __grid_constant__ StepArgs<typename S::R> a) {
   using R = typename S::R;
   const int tt = __ldg(a.step_base) + a.step_off;
+  if (tt >= a.step_end) return;
   const Roles<R> r = roles<S>(a, tt);
   face_point<S>(a, r, (R)__ldg(a.src + tt), tt, blockIdx.x * 256 + threadIdx.x, true);
 }
@@ -643,6 +644,7 @@ __global__ void __launch_bounds__(step_threads<S, TJ>(), MinBlocks<typename S::R
   unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
 
   const int tt = __ldg(a.step_base) + a.step_off;
+  if (tt >= a.step_end) return;  // a batched instance past its budget
   const Roles<R> r = roles<S>(a, tt);
   const R s = (R)__ldg(a.src + tt);
   const int tid = threadIdx.y * TK + threadIdx.x;

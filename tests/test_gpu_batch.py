@@ -1,6 +1,7 @@
-"""Batched instances (one persistent launch for many crystals) against the
-same instances stepped alone: every field and surface record must be
-bit-identical, whatever the mix, the budgets and the join/leave order."""
+"""Batched instances (one persistent launch for many crystals, or every
+instance's own kernels on worker streams) against the same instances stepped
+alone: every field and surface record must be bit-identical, whatever the
+mix, the tiles, the budgets and the join/leave order."""
 import numpy as np
 import pytest
 
@@ -28,8 +29,9 @@ def _state(sim):
     return [sim.download(k) for k in ("ux", "uy", "uz")], sim.read_surface()
 
 
+@pytest.mark.parametrize("streams", [0, 3])
 @pytest.mark.parametrize("precision", ["f32k", "f64", "f64v"])
-def test_batch_bit_identical_to_alone(gpu_lib, precision):
+def test_batch_bit_identical_to_alone(gpu_lib, precision, streams):
     from phonomena_gb300.batch import Batch
 
     alone = []
@@ -39,7 +41,7 @@ def test_batch_bit_identical_to_alone(gpu_lib, precision):
         alone.append(_state(s))
         s.close()
     sims = [_sim(cells, q, precision, 60) for q, cells in enumerate(SHAPES)]
-    with Batch(8, precision=precision, tile_j=8) as b:
+    with Batch(8, precision=precision, tile_j=8, streams=streams) as b:
         slots = [b.add(s, n) for s, n in zip(sims, BUDGETS)]
         b.step(25)
         b.step(1)
@@ -56,7 +58,8 @@ def test_batch_bit_identical_to_alone(gpu_lib, precision):
         s.close()
 
 
-def test_batch_join_and_leave(gpu_lib):
+@pytest.mark.parametrize("streams", [0, 2])
+def test_batch_join_and_leave(gpu_lib, streams):
     """Instances joining and leaving between calls (continuous batching)."""
     from phonomena_gb300.batch import Batch
 
@@ -67,7 +70,7 @@ def test_batch_join_and_leave(gpu_lib):
         ref.append(_state(s))
         s.close()
     sims = [_sim(SHAPES[q], 10 + q, "f32k", 60) for q in range(3)]
-    with Batch(2, precision="f32k") as b:
+    with Batch(2, precision="f32k", streams=streams) as b:
         s0 = b.add(sims[0], 50)
         b.step(20)
         s1 = b.add(sims[1], 50)
@@ -86,6 +89,57 @@ def test_batch_join_and_leave(gpu_lib):
             assert np.array_equal(a, e)
         assert np.array_equal(got[1], ref[q][1])
         s.close()
+
+
+@pytest.mark.parametrize("precision", ["f32k", "f64"])
+def test_streams_scheme_mixed_tiles(gpu_lib, precision):
+    """Streams scheme: each instance keeps its own tile height and x segments."""
+    from phonomena_gb300.batch import Batch
+
+    tiles = [(4, 16), (16, [20, 10, 3]), (8, -12), (4, 8), (16, 24)]
+    alone = []
+    for q, ((cells, n), (tj, xs)) in enumerate(zip(zip(SHAPES, BUDGETS), tiles)):
+        s = _sim(cells, q, precision, 60, tile_j=tj, x_segment=xs)
+        s.step(n)
+        alone.append(_state(s))
+        s.close()
+    sims = [_sim(cells, q, precision, 60, tile_j=tj, x_segment=xs) for q, (cells, (tj, xs)) in enumerate(zip(SHAPES, tiles))]
+    with Batch(len(sims), precision=precision, streams=2) as b:
+        for s, n in zip(sims, BUDGETS):
+            b.add(s, n)
+        b.step(7)
+        b.step(60)
+        b.sync()
+    for q, s in enumerate(sims):
+        got = _state(s)
+        for a, e in zip(got[0], alone[q][0]):
+            assert np.array_equal(a, e), f"instance {q}: field differs from the alone run"
+        assert np.array_equal(got[1], alone[q][1]), f"instance {q}: surface differs"
+        s.close()
+
+
+def test_set_mode_guards(gpu_lib):
+    from phonomena_gb300 import _lib
+    from phonomena_gb300._lib import PhonoError, check
+    from phonomena_gb300.batch import Batch
+
+    with pytest.raises(PhonoError, match="streams"):
+        Batch(2, precision="f32k", streams=257)
+    with Batch(2, precision="f32k") as b:
+        with pytest.raises(PhonoError, match="mode"):
+            check(gpu_lib.phono_batch_set_mode(b._b, 7, 4))
+        s = _sim(SHAPES[0], 0, "f32k", 10)
+        slot = b.add(s, 10)
+        with pytest.raises(PhonoError, match="empty"):
+            check(gpu_lib.phono_batch_set_mode(b._b, _lib.BATCH_STREAMS, 4))
+        b.remove(slot)
+        check(gpu_lib.phono_batch_set_mode(b._b, _lib.BATCH_STREAMS, 4))
+        s16 = _sim(SHAPES[0], 0, "f32k", 10, tile_j=16)  # any tile height in the streams scheme
+        b.add(s16, 10)
+        b.step(10)
+        b.sync()
+        s.close()
+        s16.close()
 
 
 def test_batch_rejects_mismatched_instances(gpu_lib):
