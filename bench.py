@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--fdtd-steps", type=int, default=None)
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--batch-streams", type=int, default=64,
-                   help="batch workload: worker streams of the streams scheme (0: the persistent scheme only)")
+                   help="batch and serving: worker streams of the streams batch scheme (0: the persistent scheme only)")
     p.add_argument("--requests", type=int, default=2000, help="serve: FP32K requests")
     p.add_argument("--rate", type=float, default=0.0, help="serve: FP32K arrivals per second (0: 70%% load)")
     p.add_argument("--requests-f64", type=int, default=40, help="serve: plain FP64 requests")
@@ -469,7 +469,7 @@ def bench_batch(args, rank, world, local, torch, dist):
 SERVE_GCELL = {"f32k": 45.0, "f64": 4.0}  # batched throughputs the offered loads refer to
 
 
-def serve_stream(precision, n, rate, seed, budget_gb):
+def serve_stream(precision, n, rate, seed, budget_gb, streams=0):
     """One Poisson stream of crystal-simulation requests (config-4 size mix
     plus 5% 512x512x128-cell jobs, 500-3000 steps each, surface uz every 10
     steps) served by continuous batching under a device-memory budget:
@@ -477,7 +477,7 @@ def serve_stream(precision, n, rate, seed, budget_gb):
     from phonomena_gb300 import serve
 
     reqs = serve.poisson_stream(n, rate, seed=seed)
-    be = serve.GpuBackend(precision=precision, capacity=256, max_steps=3000)
+    be = serve.GpuBackend(precision=precision, capacity=256, max_steps=3000, streams=streams)
     srv = serve.Server(be, budget_bytes=budget_gb * 1e9, capacity=256, chunk=60)
     streamed = []
     srv.on_result = lambda r: streamed.append(r.surface.nbytes)
@@ -512,9 +512,9 @@ def bench_serve(args, rank, world, local, torch, dist):
     rate64 = rate32 * SERVE_GCELL["f64"] / SERVE_GCELL["f32k"]
     bus = getattr(torch.cuda.get_device_properties(local), "pci_bus_id", "")
     with ClockSampler(bus) as clk:
-        r32 = serve_stream("f32k", args.requests, rate32, rank, args.budget_gb)
+        r32 = serve_stream("f32k", args.requests, rate32, rank, args.budget_gb, streams=args.batch_streams)
     clocks = clk.summary()
-    r64 = serve_stream("f64", args.requests_f64, rate64, rank + 1000, args.budget_gb)
+    r64 = serve_stream("f64", args.requests_f64, rate64, rank + 1000, args.budget_gb, streams=args.batch_streams)
     if rank == 0:
         line = {
             "metric": "served Gcell-updates/s", "value": round(r32["gcell_updates_per_s"], 4),
@@ -546,10 +546,11 @@ def serve_study(args, rank):
     for q, load in enumerate(loads):
         rate = serve.rate_for_load(SERVE_GCELL["f32k"], load)
         out["f32k"].append(serve_summary(serve_stream("f32k", args.serve_requests, rate, rank + 10 * q,
-                                                      args.budget_gb), load))
+                                                      args.budget_gb, streams=args.batch_streams), load))
     rate64 = serve.rate_for_load(SERVE_GCELL["f64"], 0.7)
     out["fp64"].append(serve_summary(serve_stream("f64", args.serve_requests_f64, rate64, rank + 1000,
-                                                  args.budget_gb), 0.7))
+                                                  args.budget_gb, streams=args.batch_streams), 0.7))
+    out["batch_scheme"] = "streams" if args.batch_streams > 0 else "persistent"
     return out
 
 

@@ -310,9 +310,11 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch **ou
  * launch above, every instance at the batch's tile_j.  PHONO_BATCH_STREAMS:
  * every instance runs its own step kernels (those of phono_step, with its own
  * tile_j and x segments) on one of `streams` worker streams (1..256), so that
- * instances run side by side; a step is done when every worker stream is.
- * The graph of 12 steps is captured again whenever the set of active
- * instances changes.  Results are those of phono_step in both schemes. */
+ * instances run side by side.  Each instance replays its own graph of 12
+ * steps (captured when it joins) and starts its next chunk as soon as its
+ * previous one is done; phono_batch_step returns once every worker's work is
+ * queued and the batch stream waits for all of them.  Results are those of
+ * phono_step in both schemes. */
 #define PHONO_BATCH_PERSISTENT 0
 #define PHONO_BATCH_STREAMS 1
 int phono_batch_set_mode(phono_batch *b, int mode, int streams);

@@ -9,10 +9,11 @@ scheme.  Two launch schemes:
   face launch for all instances;
 * streams (``streams=W``): every instance runs its own step kernels, with
   its own tile height and x segments, on one of W worker streams, so that
-  the instances' launches run side by side on the GPU.
+  the instances' launches run side by side on the GPU; each instance
+  replays its own 12-step graph (captured when it joins) and does not wait
+  for the others between chunks.
 
-Chunks of 12 steps are replayed from a captured CUDA graph (in the streams
-scheme captured again when the set of active instances changes).  Instances
+Chunks of 12 steps are replayed from captured CUDA graphs.  Instances
 keep their own step counters and budgets, so a batch can hold simulations of
 different sizes at different points of their runs, and instances can join
 and leave between calls.  Results are those of stepping each alone.

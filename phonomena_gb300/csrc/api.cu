@@ -28,6 +28,8 @@ cudaError_t launch_inclusion_ids(uint8_t* mat, const Geo& g, const double* x, co
                                  const int* kend, const uint8_t* id, int n, uint8_t host, cudaStream_t st);
 
 __global__ void advance_step_kernel(int* p, int n) { *p += n; }
+// a batched instance's step counter, stopping at its budget
+__global__ void advance_clamped_kernel(int* p, int n, int end) { *p = min(*p + n, end); }
 }  // namespace phono
 
 using namespace phono;
@@ -1154,7 +1156,16 @@ struct phono_batch {
   cudaEvent_t fork = nullptr;
   std::vector<int> order;     // active slots, costliest first
   std::vector<int> step_end;  // per slot: the instance's budget end
+  std::vector<cudaGraphExec_t> igraph;  // streams scheme: per slot, 12 steps with its budget baked in
+  cudaStream_t capture = nullptr;       // streams scheme: capture stream (always idle)
 };
+
+static void drop_igraph(phono_batch* b, int s) {
+  if (s < (int)b->igraph.size() && b->igraph[s]) {
+    cudaGraphExecDestroy(b->igraph[s]);
+    b->igraph[s] = nullptr;
+  }
+}
 
 // a handle destroyed while in a batch leaves it (the batch's work list is
 // rebuilt before its next step)
@@ -1165,6 +1176,7 @@ static void batch_detach(phono_batch* b, const phono_handle* h) {
       b->slot[s] = nullptr;
       b->remaining[s] = 0;
       b->dirty = true;
+      drop_igraph(b, s);
     }
 }
 
@@ -1174,12 +1186,15 @@ static void batch_release(phono_batch* b) {
   for (phono_handle* h : b->slot)
     if (h) h->batch = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaGraphExec_t g : b->igraph)
+    if (g) cudaGraphExecDestroy(g);
   for (void* p : b->allocs) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
   for (cudaStream_t w : b->workers) cudaStreamDestroy(w);
+  if (b->capture) cudaStreamDestroy(b->capture);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -1215,8 +1230,15 @@ static int batch_rebuild(phono_batch* b) {
   std::vector<int> act;
   for (int s = 0; s < b->cap; s++)
     if (b->slot[s] && b->remaining[s] > 0) act.push_back(s);
+  // persistent scheme: the largest instances' work items first (the tail of
+  // each step launch); streams scheme: the most remaining work first (node
+  // updates left), each instance's chunks queued before the next one's
+  auto cost = [&](int x) {
+    const phono_handle* h = b->slot[x];
+    return b->streams ? (long long)h->d.nx * h->d.ny * h->d.nz * b->remaining[x] : (long long)h->n_tile;
+  };
   std::sort(act.begin(), act.end(), [&](int x, int y) {
-    long long cx = (long long)b->slot[x]->n_tile, cy = (long long)b->slot[y]->n_tile;
+    const long long cx = cost(x), cy = cost(y);
     return cx != cy ? cx > cy : x < y;
   });
   std::vector<int2> items;
@@ -1231,10 +1253,6 @@ static int batch_rebuild(phono_batch* b) {
   }
   prefix.push_back(fb);
   b->order = act;
-  if (b->streams && b->graph) {  // the captured launches name the old instances
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
   if ((int)items.size() > b->item_cap) {
     int cap = std::max<int>((int)items.size(), 2 * b->item_cap);
     void* p = nullptr;
@@ -1276,24 +1294,7 @@ static cudaError_t chain_launch(phono_batch* b, int s, int step_off, cudaStream_
                                      : launch_step_f64v(a, h->tj, h->separate_faces, st);
 }
 
-// n steps of every active instance.  Streams scheme: instance q (costliest
-// first) on worker q mod W, forked from and joined back into the batch stream
-// with events (in a graph capture, the same events make the graph's edges).
 static cudaError_t batch_launch_steps(phono_batch* b, int first_off, int n) {
-  if (b->streams) {
-    cudaError_t e = cudaEventRecord(b->fork, b->stream);
-    const int nw = std::min<int>((int)b->order.size(), b->streams);
-    for (int w = 0; w < nw && e == cudaSuccess; w++) e = cudaStreamWaitEvent(b->workers[w], b->fork, 0);
-    for (int q = 0; q < (int)b->order.size() && e == cudaSuccess; q++)
-      for (int s = 0; s < n && e == cudaSuccess; s++) e = chain_launch(b, b->order[q], first_off + s, b->workers[q % nw]);
-    for (int w = 0; w < nw && e == cudaSuccess; w++) {
-      e = cudaEventRecord(b->joins[w], b->workers[w]);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[w], 0);
-    }
-    if (e != cudaSuccess) return e;
-    BatchArgs<float> ba = batch_args(b, 0);
-    return batch_advance_any(b->precision, &ba, b->cap, n, b->stream);
-  }
   for (int s = 0; s < n; s++) {
     BatchArgs<float> ba = batch_args(b, first_off + s);
     cudaError_t e = batch_step_any(b->precision, &ba, b->tj, b->grid_tiles, b->grid_faces, b->stream);
@@ -1301,6 +1302,88 @@ static cudaError_t batch_launch_steps(phono_batch* b, int first_off, int n) {
   }
   BatchArgs<float> ba = batch_args(b, 0);
   return batch_advance_any(b->precision, &ba, b->cap, n, b->stream);
+}
+
+// Streams scheme: the 12-step graph of the instance in slot s (its own step
+// kernels, as phono_step launches them, and a step-counter update clamped at
+// its budget), captured on the batch's idle capture stream
+static int capture_instance(phono_batch* b, int s) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < kGraphSteps && e == cudaSuccess; q++) e = chain_launch(b, s, q, b->capture);
+  if (e == cudaSuccess) {
+    advance_clamped_kernel<<<1, 1, 0, b->capture>>>(b->slot[s]->step_base, kGraphSteps, b->step_end[s]);
+    e = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamEndCapture(b->capture, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(PHONO_ERR_CUDA, std::string("instance graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  e = cudaGraphInstantiate(&b->igraph[s], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return PHONO_OK;
+}
+
+// Streams scheme: n steps of every active instance.  Instance q (costliest
+// first) runs on worker q mod W; the host issues chunk by chunk (a 12-step
+// instance graph each, then the remainder step by step) across the instances
+// so that the workers progress together, and joins the workers back into the
+// batch stream only after the last chunk: an instance's next chunk starts as
+// soon as its previous one is done, whatever the others are doing.
+static cudaError_t streams_steps(phono_batch* b, int n) {
+  const int na = (int)b->order.size(), nw = std::min(na, b->streams);
+  cudaError_t e = cudaEventRecord(b->fork, b->stream);
+  for (int w = 0; w < nw && e == cudaSuccess; w++) e = cudaStreamWaitEvent(b->workers[w], b->fork, 0);
+  const int full = n / kGraphSteps, rem = n % kGraphSteps;
+  for (int c = 0; c < full && e == cudaSuccess; c++)
+    for (int q = 0; q < na && e == cudaSuccess; q++) {
+      const int s = b->order[q];
+      if (b->remaining[s] > c * kGraphSteps) e = cudaGraphLaunch(b->igraph[s], b->workers[q % nw]);
+    }
+  for (int t = 0; t < rem && e == cudaSuccess; t++)
+    for (int q = 0; q < na && e == cudaSuccess; q++) {
+      const int s = b->order[q];
+      if (b->remaining[s] > full * kGraphSteps + t) e = chain_launch(b, s, t, b->workers[q % nw]);
+    }
+  for (int q = 0; rem && q < na && e == cudaSuccess; q++) {
+    const int s = b->order[q];
+    if (b->remaining[s] <= full * kGraphSteps) continue;
+    advance_clamped_kernel<<<1, 1, 0, b->workers[q % nw]>>>(b->slot[s]->step_base, rem, b->step_end[s]);
+    e = cudaGetLastError();
+  }
+  for (int w = 0; w < nw && e == cudaSuccess; w++) {
+    e = cudaEventRecord(b->joins[w], b->workers[w]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->joins[w], 0);
+  }
+  return e;
+}
+
+// Persistent scheme: 12-step graphs of the batch-wide launches (captured
+// once: the launches read the work list from device memory), then the
+// remainder step by step
+static int persistent_steps(phono_batch* b, int nsteps) {
+  if (!b->graph && nsteps >= kGraphSteps) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = batch_launch_steps(b, 0, kGraphSteps);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return fail(PHONO_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  CK(cudaEventRecord(b->ev0, b->stream));
+  const int full = nsteps / kGraphSteps, rem = nsteps % kGraphSteps;
+  for (int q = 0; q < full; q++) CK(cudaGraphLaunch(b->graph, b->stream));
+  if (rem) CK(batch_launch_steps(b, 0, rem));
+  CK(cudaEventRecord(b->ev1, b->stream));
+  return PHONO_OK;
 }
 
 extern "C" {
@@ -1321,6 +1404,7 @@ int phono_batch_create(int capacity, int precision, int tile_j, phono_batch** ou
   b->slot.assign(capacity, nullptr);
   b->remaining.assign(capacity, 0);
   b->step_end.assign(capacity, 0);
+  b->igraph.assign(capacity, nullptr);
 #define BTRY(x)              \
   do {                       \
     int r_ = (x);            \
@@ -1376,6 +1460,7 @@ int phono_batch_set_mode(phono_batch* b, int mode, int streams) {
   }
   const int want = mode == PHONO_BATCH_STREAMS ? streams : 0;
   if (!b->fork && want) CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  if (!b->capture && want) CK(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
   while ((int)b->workers.size() < want) {  // worker streams are kept for the batch's lifetime
     cudaStream_t w = nullptr;
     cudaEvent_t j = nullptr;
@@ -1435,6 +1520,7 @@ int phono_batch_remove(phono_batch* b, int s) {
   b->slot[s] = nullptr;
   b->remaining[s] = 0;
   b->dirty = true;
+  drop_igraph(b, s);
   return PHONO_OK;
 }
 
@@ -1453,24 +1539,20 @@ int phono_batch_step(phono_batch* b, int nsteps) {
     int rc = batch_rebuild(b);
     if (rc) return rc;
   }
-  if (!b->graph && nsteps >= kGraphSteps) {
-    cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = batch_launch_steps(b, 0, kGraphSteps);
-    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-    if (e != cudaSuccess || e2 != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return fail(PHONO_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
-    }
-    e = cudaGraphInstantiate(&b->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(PHONO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  if (b->streams) {
+    if (nsteps >= kGraphSteps)
+      for (int s : b->order)
+        if (!b->igraph[s]) {
+          int rc = capture_instance(b, s);
+          if (rc) return rc;
+        }
+    CK(cudaEventRecord(b->ev0, b->stream));
+    CK(streams_steps(b, nsteps));
+    CK(cudaEventRecord(b->ev1, b->stream));
+  } else {
+    int rc = persistent_steps(b, nsteps);
+    if (rc) return rc;
   }
-  CK(cudaEventRecord(b->ev0, b->stream));
-  const int full = nsteps / kGraphSteps, rem = nsteps % kGraphSteps;
-  for (int q = 0; q < full; q++) CK(cudaGraphLaunch(b->graph, b->stream));
-  if (rem) CK(batch_launch_steps(b, 0, rem));
-  CK(cudaEventRecord(b->ev1, b->stream));
   b->timed = true;
   for (int s = 0; s < b->cap; s++) {
     if (!b->slot[s] || b->remaining[s] <= 0) continue;

@@ -96,14 +96,14 @@ class GpuBackend:
     ``max_steps`` steps so that requests of any length share a key.
     """
 
-    def __init__(self, precision="f32k", capacity=128, tile_j=16, x_segment=0, max_steps=3000):
+    def __init__(self, precision="f32k", capacity=128, tile_j=16, x_segment=0, max_steps=3000, streams=0):
         from .batch import Batch
 
         self.precision = precision
         self.tile_j = tile_j
         self.x_segment = x_segment
         self.max_steps = int(max_steps)
-        self.batch = Batch(capacity, precision=precision, tile_j=tile_j)
+        self.batch = Batch(capacity, precision=precision, tile_j=tile_j, streams=streams)
         self.pool = {}  # key -> [DeviceSimulation], least recently used first
         self._lru = []  # keys of pooled simulations, least recently used first
 
