@@ -3,7 +3,8 @@
 Builds the crystal (lattice a=16, radii U[0.2a, 0.4a], 25% tungsten, 42 MHz
 line source), steps it with the chosen scheme and tile shape, and prints the
 device time, Gcell-updates/s and the energy.  With ``--batch N`` it runs N
-crystals of the batching mix in one batch instead.  Used as the fixed command
+crystals of the batching mix in one batch instead (``--batch-streams W``:
+the streams scheme on W worker streams).  Used as the fixed command
 for profiling the kernels.
 """
 from __future__ import annotations
@@ -23,6 +24,8 @@ def main(argv=None):
     p.add_argument("--x-segment", type=int, default=32)
     p.add_argument("--x-segments", default="", help="explicit x segment lengths, comma separated (phono_set_segments)")
     p.add_argument("--batch", type=int, default=0, help="run this many crystals of the batching mix instead")
+    p.add_argument("--batch-streams", type=int, default=0,
+                   help="with --batch: worker streams of the streams scheme (0: the persistent kernel)")
     p.add_argument("--seed", type=int, default=0)
     a = p.parse_args(argv)
 
@@ -42,7 +45,7 @@ def main(argv=None):
                                  max_steps=a.steps, record_every=10, tile_j=a.tile_j, x_segment=a.x_segment)
             s.set_source(crystal.sin_source(sp.freq, m.dt, a.steps))
             sims.append(s)
-        with Batch(len(sims), precision=a.precision, tile_j=a.tile_j) as b:
+        with Batch(len(sims), precision=a.precision, tile_j=a.tile_j, streams=a.batch_streams) as b:
             for s in sims:
                 b.add(s, a.steps)
             b.step(a.steps)
@@ -51,7 +54,8 @@ def main(argv=None):
         nodes = sum(sp.n_nodes for sp in specs)
         for s in sims:
             s.close()
-        print(json.dumps({"instances": a.batch, "nodes": nodes, "steps": a.steps, "ms": round(ms, 3),
+        print(json.dumps({"instances": a.batch, "batch_streams": a.batch_streams, "nodes": nodes, "steps": a.steps,
+                          "ms": round(ms, 3),
                           "gcell_updates_per_s": round(nodes * a.steps / ms / 1e6, 3)}))
         return 0
 
