@@ -164,6 +164,19 @@ def traffic_per_node(kernel):
     return d.get(kernel, {}).get("dram_bytes_per_node")
 
 
+def traffic_bounds(scheme, nodes):
+    """DRAM bytes per batch step bounded from the committed ncu summary where
+    the scheme's traffic is not observable directly (streams: ncu serialises
+    the side-by-side launches); None for the persistent scheme."""
+    if scheme == "persistent":
+        return None
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    b = json.load(open(p)).get("fdtd_step_kernel_f32k_batch", {}).get("bounds_bytes_per_node")
+    return [round(v * nodes) for v in b] if b else None
+
+
 def cpu_oracle_rate(cells, seconds, seed=0):
     """FP64 reference restatement on all host threads: (Gcell-updates/s, threads, steps)."""
     from oracle import cpu_oracle
@@ -449,6 +462,7 @@ def bench_batch(args, rank, world, local, torch, dist):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved / hbm_peak, 4), "peak_kind": peak_kind,
                          "traffic": (round(tpn * node_sum) if tpn else None),
+                         "traffic_bounds_per_launch": traffic_bounds(scheme, node_sum),
                          "algorithmic_bytes_per_launch": BYTES_PER_NODE * node_sum,
                          "avg_launch_ms": round(launch_ms, 5),
                          "launch_timing": ("one time step = persistent tile launch + batched face launch "
