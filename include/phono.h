@@ -263,9 +263,9 @@ int phono_energy(phono_handle *h, double out[2]);
  * stream, or events).  Every call overwrites the partials it reads, so
  * nothing has to be cleared between calls.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  The
- * address is cached for the life of the device's primary context: do not
- * call this again on a device after cudaDeviceReset.
+ * device current.  The address is cached for the life of the device's
+ * primary context: do not call this again on a device after
+ * cudaDeviceReset.
  *
  * Inputs are dense arrays in the reference shapes, element type given by
  * `precision`, all device pointers; out_dev receives two doubles
