@@ -24,13 +24,13 @@ def _requests():
     return out
 
 
-@pytest.mark.parametrize("precision", ["f32k", "f64"])
-def test_served_equals_alone(gpu_lib, precision):
+@pytest.mark.parametrize("precision,streams", [("f32k", 0), ("f64", 0), ("f32k", 2)])
+def test_served_equals_alone(gpu_lib, precision, streams):
     from phonomena_gb300 import serve
     from phonomena_gb300.device import DeviceSimulation
 
     reqs = _requests()
-    be = serve.GpuBackend(precision=precision, capacity=3, max_steps=120)
+    be = serve.GpuBackend(precision=precision, capacity=3, max_steps=120, streams=streams)
     budget = 3.2 * be.footprint((57, 49, 21), 120, 5)  # forces queueing and pool eviction
     srv = serve.Server(be, budget_bytes=budget, capacity=3, chunk=24)
     streamed = []
