@@ -291,17 +291,19 @@ typedef struct phono_energy_dense {
 
 int phono_energy_static(const phono_energy_dense *in, double *out_dev, void *stream);
 
-/* Batches: many simulations stepped together.  Every time step is one
- * persistent tile launch (CTAs pull (instance, tile) work items until none
- * are left) and one face launch for all active instances, replayed from a
- * captured CUDA graph.  The reference runs one simulation per solver object
- * (base_solver.py:245-266) and has no counterpart; the per-instance
+/* Batches: many simulations stepped together.  In the default (persistent)
+ * scheme every time step is one persistent tile launch (CTAs pull (instance,
+ * tile) work items until none are left) and one face launch for all active
+ * instances, replayed from a captured CUDA graph; phono_batch_set_mode
+ * selects the other scheme.  The reference runs one simulation per solver
+ * object (base_solver.py:245-266) and has no counterpart; the per-instance
  * arithmetic is that of phono_step, bit for bit.  Instances are handles made
  * by phono_create with the batch's precision and ny >= 4 (and the batch's
- * tile_j in the persistent scheme); each keeps its own x segments.  While a handle is in a batch, phono_step,
- * phono_reset, phono_set_materials, phono_upload and phono_set_tiling on it
- * return PHONO_ERR_STATE; call phono_batch_sync before reading it.  A handle
- * destroyed while in a batch leaves the batch. */
+ * tile_j in the persistent scheme); each keeps its own x segments.  While a
+ * handle is in a batch, phono_step, phono_reset, phono_set_materials,
+ * phono_upload and phono_set_tiling on it return PHONO_ERR_STATE; call
+ * phono_batch_sync before reading it.  A handle destroyed while in a batch
+ * leaves the batch. */
 typedef struct phono_batch phono_batch;
 
 int phono_batch_create(int capacity, int precision, int tile_j, phono_batch **out);
